@@ -1,0 +1,421 @@
+"""Benchmark of the CENTRE entropy hot path on GB300.
+
+One step = the whole hot path over one synthetic trajectory already resident
+in HBM: histogram discretisation of every bond/angle/torsion, 1-D counts and
+entropies, 2-D joint counts and entropies of every DOF pair, MI, MIE sums and
+the MIST spanning tree.  Workload: a 1000-atom chain (999 bonds, 998 angles,
+997 torsions = 2994 DOFs, 4,480,521 pairs), 100,000 frames, 50 bins per DOF,
+10 convergence steps, ML estimator, Jacobian on.  The metric is MI pairs/s.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--form tc|atomic|auto]
+    python bench.py --impl reference      # the CPU implementation of the path
+
+Multi-GPU (torchrun): every rank runs its own independent trajectory
+(replicas; no collective on the data path); value = all ranks' pairs / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MI pairs/s"
+UNIT = "pairs/s"
+NBINS = 50
+NSTEPS = 10
+
+
+def workload(name):
+    from centre_gb300.synth import WORKLOADS
+    w = dict(WORKLOADS[name])
+    na = w["natoms"]
+    w["ndof"] = 3 * na - 6
+    w["npairs"] = w["ndof"] * (w["ndof"] - 1) // 2
+    return w
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- CPU port --
+def cpu_sample_rate(tr, target_s=8.0, nthreads=None, seed=0):
+    """Time the CPU oracle (restatement of the reference, OpenMP over pairs)
+    on a bounded sample of the workload; returns (pairs/s extrapolated to the
+    whole workload, details)."""
+    import oracle
+    oracle.build(with_ref=False)
+    orc = oracle.Oracle()
+    nthreads = nthreads or os.cpu_count()
+    blocks = list(tr.blocks())
+    # discretise a DOF sample of each type
+    t0 = time.perf_counter()
+    nd = 0
+    bins_l, ext_l, types_l = [], [], []
+    for typ, blk in blocks:
+        k = min(len(blk), 24)
+        b, e = orc.discretize(typ, blk[:k], [NBINS], nthreads=nthreads)
+        bins_l.append(b)
+        ext_l.append(e)
+        types_l += [typ] * k
+        nd += k
+    t_disc = (time.perf_counter() - t0) / nd
+    bins = np.concatenate(bins_l)
+    ext = np.concatenate(ext_l)
+    types = np.array(types_l, np.uint8)
+    t0 = time.perf_counter()
+    orc.entropy1d(types, bins, ext, NSTEPS, [NBINS], [0], True, nthreads=nthreads)
+    t_1d = (time.perf_counter() - t0) / len(types)
+    rng = np.random.default_rng(seed)
+    n = len(types)
+    # calibrate the pair sample to ~target_s seconds
+    npair = 64
+    t_pair = None
+    spent = 0.0
+    while True:
+        pairs = rng.integers(0, n, size=(npair, 2)).astype(np.uint32)
+        pairs = pairs[pairs[:, 0] != pairs[:, 1]]
+        t0 = time.perf_counter()
+        orc.entropy2d(pairs, types, bins, ext, NSTEPS, [NBINS], [0], True, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        spent += dt
+        t_pair = dt / len(pairs)
+        if dt > target_s / 4 or spent > target_s:
+            break
+        npair = int(npair * min(8.0, max(2.0, (target_s / 3) / max(dt, 1e-3))))
+    return t_disc, t_1d, t_pair, len(pairs), nthreads
+
+
+def cpu_pairs_per_s(w, t_disc, t_1d, t_pair):
+    total = w["ndof"] * (t_disc + t_1d) + w["npairs"] * t_pair
+    return w["npairs"] / total
+
+
+# ------------------------------------------------------------ our GPU arm --
+def run_ours(args):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from centre_gb300.api import Context, make_params
+    from centre_gb300.synth import chain_trajectory
+
+    w = workload(args.workload)
+    tr = chain_trajectory(w["natoms"], w["nframes"], seed=1000 + rank, coupling=w["coupling"])
+    dev = torch.device("cuda", local)
+    blocks = [(typ, torch.from_numpy(blk).to(dev)) for typ, blk in tr.blocks()]
+    ndof = sum(b.shape[0] for _, b in blocks)
+    n = tr.nframes
+    npairs = ndof * (ndof - 1) // 2
+    types = torch.tensor(sum([[t] * b.shape[0] for t, b in blocks], []), dtype=torch.uint8,
+                         device=dev)
+    bins = torch.empty((ndof, 1, n), dtype=torch.uint8, device=dev)
+    ext = torch.empty((ndof, 4), dtype=torch.float64, device=dev)
+    s1 = torch.empty((ndof, 1, 1, NSTEPS), dtype=torch.float64, device=dev)
+    s2 = torch.empty((npairs, 1, 1, NSTEPS), dtype=torch.float64, device=dev)
+    mi = torch.empty_like(s2)
+    form = {"auto": 0, "atomic": 1, "tc": 2}[args.form]
+
+    ctx = Context(local)
+    stream = torch.cuda.Stream(device=dev)
+    ctx.set_stream(stream.cuda_stream)
+
+    def step(f):
+        p = make_params(n, NSTEPS, [NBINS], [0], True, counts_form=f)
+        off = 0
+        for typ, data in blocks:
+            k = data.shape[0]
+            ctx.discretize_dev(typ, data, [NBINS], bins[off:off + k], ext[off:off + k])
+            off += k
+        ctx.entropy1d_dev(p, types, bins, ext, s1)
+        ctx.entropy2d_dev(p, types, bins, ext, s2)
+        return ctx.score_dev(p, types, s1, s2, None, True, mi)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step(form)
+    barrier()
+    ctx.enable_timing(True)
+    launches0 = ctx.launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            res = step(form)
+        ev1.record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+    ms = ev0.elapsed_time(ev1)
+    # score_dev synchronises internally for the tree, so the device clock
+    # and the host clock agree up to launch gaps; report the larger
+    step_ms = max(ms, wall * 1e3) / args.steps
+    launches = ctx.launches - launches0
+    t_disc, n_disc = ctx.timer(0)
+    t_1d, n_1d = ctx.timer(1)
+    t_pairs, n_pairs = ctx.timer(2)
+    t_score, n_score = ctx.timer(3)
+    ctx.enable_timing(False)
+
+    t = torch.tensor([step_ms], device=dev)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    step_ms = float(t.item())
+    value = world * npairs / (step_ms / 1e3)
+
+    hbm, bf16, src = peaks()
+    fp8_peak = 2.0 * bf16
+    used = NSTEPS * (n // NSTEPS)
+    flops_per_launch = 2.0 * used * NBINS * NBINS * npairs
+    pair_ms = t_pairs / max(n_pairs, 1)
+    achieved = flops_per_launch / (pair_ms / 1e3) / 1e12
+    disc_ms = t_disc / max(n_disc, 1)
+    # discretise launches cover one DOF block each; bytes per launch averaged
+    disc_bytes = 5.0 * ndof * n / 3
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded BAT chain, float32)",
+        "config": {"workload": f"chain{w['natoms']}: {ndof} DOFs, {n} frames, {NBINS} bins, "
+                               f"{NSTEPS} steps, ML, all {npairs} pairs, MIE-2 + MIST",
+                   "counts_form": args.form, "l2": "inputs (1.2 GB) larger than L2",
+                   "parallelism": f"replicas x{world}"},
+        "mist_wall_ms": t_score / max(args.steps, 1),
+        "kernel_ms_per_step": {"discretize": t_disc / args.steps, "counts1d": t_1d / args.steps,
+                               "pair_counts": t_pairs / args.steps,
+                               "score_mst": t_score / args.steps},
+        "roofline": {"bound": "tensor", "kernel": "pair counts", "achieved": achieved,
+                     "peak": fp8_peak, "unit": "TFLOP/s", "frac": achieved / fp8_peak,
+                     "traffic": None,
+                     "note": f"2*N*B^2 flops per pair (B={NBINS} real bins); fp8 peak = 2 x "
+                             f"{src} bf16 {bf16:.0f} TF/s"},
+        "discretize_roofline": {"bound": "hbm", "achieved": disc_bytes / (disc_ms / 1e3) / 1e9,
+                                "peak": hbm, "unit": "GB/s",
+                                "frac": disc_bytes / (disc_ms / 1e3) / 1e9 / hbm,
+                                "note": f"5 B per DOF-frame; {src} peak"},
+        "gpu_launches": launches,
+    }
+    if args.form != "atomic" and args.compare_atomic:
+        # the plain atomic-histogram form on the same data, one timed step
+        step(1)
+        barrier()
+        ctx.enable_timing(True)
+        step(1)
+        ta, na_ = ctx.timer(2)
+        ctx.enable_timing(False)
+        out["atomic_pair_counts_ms"] = ta / max(na_, 1)
+        out["tc_over_atomic"] = (ta / max(na_, 1)) / pair_ms if pair_ms > 0 else None
+    clocks = clk.summary()
+    if clocks:
+        out["clocks"] = clocks
+
+    if not args.no_e2e:
+        out["e2e"] = run_e2e(ctx, tr, args, w, world, dist, dev)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        t_d, t_1, t_p, ns, cores = cpu_sample_rate(tr, target_s=args.cpu_seconds)
+        out["cpu_baseline"] = {
+            "value": cpu_pairs_per_s(w, t_d, t_1, t_p), "unit": UNIT, "cores": cores,
+            "kind": "port",
+            "sample": f"{ns} random DOF pairs x {n} frames (count+entropy) and 72 DOFs "
+                      f"discretised on {cores} host threads, extrapolated to {npairs} pairs; "
+                      "MST excluded"}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_e2e(ctx, tr, args, w, world, dist, dev):
+    """The same step through the host-pointer C ABI (the stage-by-stage
+    drop-in): pinned host BAT in, bins/entropies/MI back to host."""
+    import torch
+    from centre_gb300.api import make_params
+    n = tr.nframes
+    blocks = []
+    for typ, blk in tr.blocks():
+        h = torch.from_numpy(blk).pin_memory()
+        blocks.append((typ, h.numpy()))
+    ndof = sum(b.shape[0] for _, b in blocks)
+    npairs = ndof * (ndof - 1) // 2
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+    bins = pin((ndof, 1, n), torch.uint8)
+    ext = pin((ndof, 4), torch.float64)
+    s1 = pin((ndof, 1, 1, NSTEPS), torch.float64)
+    s2 = pin((npairs, 1, 1, NSTEPS), torch.float64)
+    mi = pin((npairs, 1, 1, NSTEPS), torch.float64)
+    types = np.array(sum([[t] * b.shape[0] for t, b in blocks], []), np.uint8)
+    form = {"auto": 0, "atomic": 1, "tc": 2}[args.form]
+    p = make_params(n, NSTEPS, [NBINS], [0], True, counts_form=form)
+
+    def step():
+        off = 0
+        for typ, data in blocks:
+            k = data.shape[0]
+            ctx.discretize(typ, data, [NBINS], bins_out=bins[off:off + k], ext_out=ext[off:off + k])
+            off += k
+        ctx.entropy1d(p, types, bins, ext, out=s1)
+        ctx.entropy2d(p, types, bins, ext, out=s2)
+        return ctx.score(p, types, s1, s2, None, True, True, mi_out=mi)
+
+    step()
+    steps = max(1, min(args.steps, 3))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = (time.perf_counter() - t0) / steps
+    t = torch.tensor([dt], device=dev)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dt = float(t.item())
+    h2d = sum(b.nbytes for _, b in blocks) + 2 * bins.nbytes + 2 * ext.nbytes + s1.nbytes \
+        + s2.nbytes + 3 * types.nbytes
+    d2h = bins.nbytes + ext.nbytes + s1.nbytes + s2.nbytes + mi.nbytes
+    return {"value": world * npairs / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3, "steps": steps}
+
+
+# ------------------------------------------------------- reference arm ----
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from centre_gb300.synth import chain_trajectory
+    w = workload(args.workload)
+    tr = chain_trajectory(w["natoms"], w["nframes"], seed=1000, coupling=w["coupling"])
+    vals = []
+    info = None
+    for k in range(args.warmup + args.steps):
+        t_d, t_1, t_p, ns, cores = cpu_sample_rate(tr, target_s=args.cpu_seconds, seed=k)
+        if k >= args.warmup:
+            vals.append(cpu_pairs_per_s(w, t_d, t_1, t_p))
+            info = (ns, cores)
+    v = float(np.median(vals))
+    ns, cores = info
+    ndof, npairs = w["ndof"], w["npairs"]
+    sample = (f"per step: {ns} random DOF pairs x {w['nframes']} frames (count+entropy) and 72 "
+              f"DOFs discretised, extrapolated to {npairs} pairs; MST excluded")
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": w["npairs"] / v * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded BAT chain, float32)",
+        "config": {"workload": f"chain{w['natoms']}: {ndof} DOFs, {w['nframes']} frames, "
+                               f"{NBINS} bins, {NSTEPS} steps, ML, all {npairs} pairs",
+                   "implementation": "CPU restatement of the reference path (oracle/), "
+                                     "OpenMP over pairs"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="auto", choices=["auto", "tc", "atomic"])
+    ap.add_argument("--workload", default="chain1000")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare-atomic", dest="compare_atomic", action="store_false")
+    ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,207 @@
+"""Python front-end over the C ABI (host numpy buffers or device tensors).
+
+``Context`` wraps one ``centre_ctx``.  Methods without a suffix take and
+return numpy arrays (the C entry points copy host<->device inside); ``*_dev``
+methods take torch CUDA tensors (device pointers, asynchronous on the
+context's stream).  Array layouts are the reference's (see
+include/centre_gpu.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import CentreError, EntropyParams, make_params, SUMS_COLS, SUMS_NAMES  # noqa: F401
+
+BOND, ANGLE, DIHEDRAL = 1, 2, 3
+ML, MM, CS, JS = 0, 1, 2, 3
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(C.c_void_p)
+    return C.c_void_p(int(a.data_ptr()))  # torch tensor
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self.L = _lib.load()
+        h = C.c_void_p()
+        rc = self.L.centre_gpu_create(C.byref(h), int(device))
+        if rc != 0:
+            raise CentreError(rc, self.L.centre_gpu_strerror(rc).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.centre_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def check(self, rc: int):
+        if rc != 0:
+            msg = self.L.centre_gpu_last_error(self.h).decode()
+            raise CentreError(rc, msg or self.L.centre_gpu_strerror(rc).decode())
+
+    @property
+    def launches(self) -> int:
+        return int(self.L.centre_gpu_launch_count(self.h))
+
+    def set_stream(self, stream_ptr: int):
+        self.check(self.L.centre_gpu_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def enable_timing(self, on: bool = True):
+        self.check(self.L.centre_gpu_enable_timing(self.h, int(bool(on))))
+
+    def timer(self, which: int):
+        """(milliseconds, launches) of a kernel class since timing was enabled:
+        0 discretise, 1 1-D counts, 2 pair counts, 3 scoring."""
+        ms = C.c_double()
+        n = C.c_uint64()
+        self.check(self.L.centre_gpu_timer(self.h, int(which), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def synchronize(self):
+        self.check(self.L.centre_gpu_synchronize(self.h))
+
+    # ---------------------------------------------------------- host API --
+    def discretize(self, bat_type, data, schemes, bins_ref=None, optimize=True, bins_out=None,
+                   ext_out=None):
+        data = _c(data, np.float32)
+        ndof, n = data.shape
+        sch = _c(schemes, np.uint8)
+        bins = bins_out if bins_out is not None else np.empty((ndof, len(sch), n), np.uint8)
+        ext = ext_out if ext_out is not None else np.empty((ndof, 4), np.float64)
+        ref = int(bins_ref if bins_ref is not None else sch[0])
+        self.check(self.L.centre_gpu_discretize(self.h, int(bat_type), _ptr(data), ndof, n,
+                                                _ptr(sch), len(sch), ref, int(bool(optimize)),
+                                                _ptr(bins), _ptr(ext)))
+        return bins, ext
+
+    def entropy1d(self, params: EntropyParams, types, bins, ext, want_freq=False, out=None):
+        bins = _c(bins, np.uint8)
+        types = _c(types, np.uint8)
+        ext = _c(ext, np.float64)
+        ndof = bins.shape[0]
+        s1 = out if out is not None else np.empty(
+            (ndof, params.nestimators, params.nschemes, params.nsteps), np.float64)
+        freq = None
+        if want_freq:
+            nsum = sum(params.bin_schemes[i] for i in range(params.nschemes))
+            freq = np.empty((ndof, params.nsteps, nsum), np.uint64)
+        self.check(self.L.centre_gpu_entropy1d(self.h, C.byref(params), ndof, _ptr(types),
+                                               _ptr(bins), _ptr(ext), _ptr(s1), _ptr(freq)))
+        return (s1, freq) if want_freq else s1
+
+    def entropy2d(self, params: EntropyParams, types, bins, ext, pairs=None, out=None):
+        bins = _c(bins, np.uint8)
+        types = _c(types, np.uint8)
+        ext = _c(ext, np.float64)
+        ndof = bins.shape[0]
+        if pairs is not None:
+            pairs = _c(pairs, np.uint32).reshape(-1, 2)
+            npairs = len(pairs)
+        else:
+            npairs = ndof * (ndof - 1) // 2
+        s2 = out if out is not None else np.empty(
+            (npairs, params.nestimators, params.nschemes, params.nsteps), np.float64)
+        self.check(self.L.centre_gpu_entropy2d(self.h, C.byref(params), ndof, _ptr(types),
+                                               _ptr(bins), _ptr(ext), npairs, _ptr(pairs),
+                                               _ptr(s2)))
+        return s2
+
+    def counts2d(self, params: EntropyParams, bins, pairs):
+        bins = _c(bins, np.uint8)
+        pairs = _c(pairs, np.uint32).reshape(-1, 2)
+        nsq = sum(params.bin_schemes[i] ** 2 for i in range(params.nschemes))
+        freq = np.empty((len(pairs), params.nsteps, nsq), np.uint64)
+        self.check(self.L.centre_gpu_counts2d(self.h, C.byref(params), bins.shape[0], _ptr(bins),
+                                              len(pairs), _ptr(pairs), _ptr(freq)))
+        return freq
+
+    def score(self, params: EntropyParams, types, s1, s2, pairs=None, build_tree=True,
+              want_mi=True, mi_out=None):
+        types = _c(types, np.uint8)
+        s1 = _c(s1, np.float64)
+        s2 = _c(s2, np.float64)
+        ndof = len(types)
+        G = params.nestimators * params.nschemes * params.nsteps
+        if pairs is not None:
+            pairs = _c(pairs, np.uint32).reshape(-1, 2)
+        npairs = s2.shape[0]
+        mi = (mi_out if mi_out is not None else np.empty_like(s2)) if want_mi else None
+        mie = np.empty((G, SUMS_COLS), np.float64)
+        mist = np.empty((G, SUMS_COLS), np.float64) if build_tree else None
+        cap = max(ndof - 1, 0)
+        tree = np.zeros((G, cap), np.uint32) if build_tree else None
+        ntree = np.zeros(G, np.uint32) if build_tree else None
+        self.check(self.L.centre_gpu_score(self.h, C.byref(params), ndof, _ptr(types), _ptr(s1),
+                                           npairs, _ptr(pairs), _ptr(s2), int(bool(build_tree)),
+                                           _ptr(mi), _ptr(mie), _ptr(mist), _ptr(tree),
+                                           _ptr(ntree)))
+        shp = (params.nestimators, params.nschemes, params.nsteps)
+        out = {"mie": mie.reshape(*shp, SUMS_COLS)}
+        if want_mi:
+            out["mi"] = mi
+        if build_tree:
+            out["mist"] = mist.reshape(*shp, SUMS_COLS)
+            out["tree"] = [tree[g, : ntree[g]].copy() for g in range(G)]
+        return out
+
+    # -------------------------------------------------------- device API --
+    def discretize_dev(self, bat_type, data, schemes, bins_out, ext_out, bins_ref=None,
+                       optimize=True):
+        """data: CUDA float32 [ndof][n]; bins_out uint8 [ndof][nsch][n]; ext_out f64 [ndof][4]."""
+        sch = _c(schemes, np.uint8)
+        ndof, n = int(data.shape[0]), int(data.shape[1])
+        ref = int(bins_ref if bins_ref is not None else sch[0])
+        self.check(self.L.centre_gpu_discretize_dev(self.h, int(bat_type), _ptr(data), ndof, n,
+                                                    _ptr(sch), len(sch), ref,
+                                                    int(bool(optimize)), _ptr(bins_out),
+                                                    _ptr(ext_out)))
+
+    def entropy1d_dev(self, params, types, bins, ext, s1_out, freq_out=None):
+        self.check(self.L.centre_gpu_entropy1d_dev(self.h, C.byref(params), int(bins.shape[0]),
+                                                   _ptr(types), _ptr(bins), _ptr(ext),
+                                                   _ptr(s1_out), _ptr(freq_out)))
+
+    def entropy2d_dev(self, params, types, bins, ext, s2_out, pairs=None):
+        ndof = int(bins.shape[0])
+        npairs = int(pairs.shape[0]) if pairs is not None else ndof * (ndof - 1) // 2
+        self.check(self.L.centre_gpu_entropy2d_dev(self.h, C.byref(params), ndof, _ptr(types),
+                                                   _ptr(bins), _ptr(ext), npairs, _ptr(pairs),
+                                                   _ptr(s2_out)))
+
+    def score_dev(self, params, types_dev, s1, s2, pairs=None, build_tree=True, mi_out=None):
+        ndof = int(types_dev.shape[0])
+        npairs = int(s2.shape[0])
+        G = params.nestimators * params.nschemes * params.nsteps
+        mie = np.empty((G, SUMS_COLS), np.float64)
+        mist = np.empty((G, SUMS_COLS), np.float64)
+        cap = max(ndof - 1, 0)
+        tree = np.zeros((G, cap), np.uint32)
+        ntree = np.zeros(G, np.uint32)
+        self.check(self.L.centre_gpu_score_dev(self.h, C.byref(params), ndof, _ptr(types_dev),
+                                               _ptr(s1), npairs, _ptr(pairs), _ptr(s2),
+                                               int(bool(build_tree)), _ptr(mi_out), _ptr(mie),
+                                               _ptr(mist), _ptr(tree), _ptr(ntree)))
+        return {"mie": mie, "mist": mist, "tree": [tree[g, : ntree[g]].copy() for g in range(G)]}

@@ -1,0 +1,114 @@
+// common.cuh -- shared definitions of the CENTRE GB300 library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "centre_gpu.h"
+
+namespace centre {
+
+// Largest bin count the reference can express (hbin_t is uint8_t,
+// src/configcentre.h:24).
+constexpr int kMaxBins = 255;
+constexpr int kMaxSchemes = 16;
+constexpr int kMaxSteps = 255;
+
+// Fixed-point scale of the per-cell c*ln(c) terms: sums of round(c ln c *
+// 2^32) are exact integers, so the joint-entropy sums are identical however
+// the cells are distributed over threads, tiles or count kernels.  With
+// counts <= 2^27 the per-step sum (<= n ln n * 2^32) fits in uint64.
+constexpr double kClncScale = 4294967296.0;
+constexpr double kClncInvScale = 1.0 / 4294967296.0;
+constexpr uint64_t kMaxFrames = 1ull << 27;
+
+// Grow-only device scratch owned by a context.
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace centre
+
+struct centre_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  uint64_t launches = 0;
+  std::string last_error;
+  centre::DevBuf scratch[8];
+  int *d_flag = nullptr;   // device error flag (bin range, timeouts)
+  int *h_flag = nullptr;   // pinned mirror
+  int cc_major = 0, cc_minor = 0;
+  unsigned long long *d_clnc = nullptr;  // round(c ln c 2^32), c < 2^16
+  // event timing of the hot kernels (centre_gpu_enable_timing)
+  bool timing = false;
+  struct TimerRec {
+    int which;
+    cudaEvent_t a, b;
+  };
+  std::vector<TimerRec> timers;
+  std::vector<cudaEvent_t> event_pool;
+  double timer_ms[4] = {0, 0, 0, 0};
+  uint64_t timer_n[4] = {0, 0, 0, 0};
+};
+
+namespace centre {
+
+// Scratch slots of a context.
+enum ScratchSlot {
+  kSlotIn = 0,     // staged host inputs
+  kSlotBins = 1,
+  kSlotOut = 2,
+  kSlotMoments = 3,  // per pair/step sum(c ln c), nnz
+  kSlotAux = 4,
+  kSlotPairs = 5,
+  kSlotAux2 = 6,
+  kSlotAux3 = 7,
+};
+
+int set_error(centre_ctx *ctx, int status, const std::string &msg);
+int check_cuda(centre_ctx *ctx, cudaError_t e, const char *what);
+void *scratch(centre_ctx *ctx, int slot, size_t bytes, int *status);
+unsigned long long *ctx_clnc(centre_ctx *ctx);
+
+// Scoped event timer around a launch on the context's stream (no-op unless
+// timing is enabled).
+struct KernelTimer {
+  centre_ctx *ctx;
+  int which;
+  cudaEvent_t a = nullptr, b = nullptr;
+  KernelTimer(centre_ctx *c, int w);
+  ~KernelTimer();
+};
+
+#define CENTRE_TRY(expr)        \
+  do {                          \
+    int _rc = (expr);           \
+    if (_rc != CENTRE_OK) return _rc; \
+  } while (0)
+
+#define CENTRE_CUDA(ctx, expr) CENTRE_TRY(::centre::check_cuda((ctx), (expr), #expr))
+
+// Device error-flag bits.
+enum : int {
+  kFlagBinRange = 1,
+  kFlagTimeout = 2,
+  kFlagDomain = 4,
+};
+
+// Order-preserving map of a double onto uint64 (larger double -> larger key).
+__host__ __device__ inline uint64_t order_key(double v) {
+  union {
+    double d;
+    uint64_t u;
+  } c;
+  c.d = v;
+  return (c.u & 0x8000000000000000ull) ? ~c.u : (c.u | 0x8000000000000000ull);
+}
+
+}  // namespace centre

@@ -1,0 +1,561 @@
+// entropy.cu -- 1-D/2-D counts and plug-in entropies.
+//
+// Reference: binData1D / binData2D (src/Estimators.cpp:56-205) and
+// entropy1D / entropy2D (:217-651), driven by EntropyCalculator::run1d /
+// run2d_xx / run2d_xy (src/EntropyCalculator.cpp:6, :281, :674).
+//
+// Joint entropy factorisation.  For the ML and MM estimators the reference's
+// per-cell sum (src/Estimators.cpp:586-642)
+//     S = -A * sum_{c>0} J1 J2 p log p,   p = c / (n A J1 J2)
+// equals, term by term,
+//     S = log n + log A - (1/n) sum c ln c + (1/n)(L_i + L_j)
+// with L_i = sum_b R_b ln J_i(b) over the DOF's own 1-D counts R (the row
+// marginal of the joint table is the 1-D histogram of the same frames).  So
+// per pair and step only two integers are needed: sum over cells of
+// round(c ln c * 2^32) (exact, order independent) and the number of
+// non-empty cells (for Miller-Madow).  Both count kernels (shared-memory
+// atomics here, tensor-core one-hot in pairs_tc.cu) produce exactly these
+// integers, so their entropies are bit-identical.  The Chao-Shen and
+// James-Stein estimators need every cell; they take the counts path
+// (materialised joint counts + per-cell evaluation, as the reference).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "entropy.cuh"
+
+namespace centre {
+
+// ----------------------------------------------------------------------------
+// c*ln(c) fixed-point table
+__global__ void clnc_table_kernel(unsigned long long *t, int n) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) t[c] = clnc_fixed((unsigned)c);
+}
+
+// ----------------------------------------------------------------------------
+// 1-D: counts per step, cumulative; entropies for every estimator; L sums.
+// One CTA per (DOF, scheme).
+__global__ void __launch_bounds__(256)
+entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ types,
+                 const double *__restrict__ ext, const __grid_constant__ EntParams P,
+                 double *__restrict__ s1, unsigned long long *__restrict__ freq_out,
+                 double *__restrict__ lsum, int *__restrict__ flag) {
+  const int dof = blockIdx.x / P.nschemes;
+  const int s = blockIdx.x % P.nschemes;
+  const int nb = P.schemes[s];
+  const uint64_t n = P.nframes, ss = P.step_size;
+  const uint8_t *row = bins + ((uint64_t)dof * P.nschemes + s) * n;
+  __shared__ unsigned hist[256];
+  __shared__ unsigned long long cum[256];
+  __shared__ double mids[256];
+  __shared__ int badrange;
+  const int tid = threadIdx.x;
+  if (tid == 0) badrange = 0;
+  for (int b = tid; b < 256; b += blockDim.x) cum[b] = 0;
+  const int type = types[dof];
+  const double mn = ext[4 * dof], mx = ext[4 * dof + 1];
+  double w = __ddiv_rn(__dsub_rn(mx, mn), (double)nb);
+  const double hw = w / 2;
+  if (P.kde) w = 1.0;
+  const bool hj = (type == 1 || type == 2);
+  for (int b = tid; b < nb; b += blockDim.x)
+    mids[b] = hj ? __dadd_rn(__dadd_rn(mn, __dmul_rn((double)b, w)), hw) : 0.0;
+  const int nsum = P.nbins_sum;
+  const int off = P.scheme_off[s];
+  const uint64_t per = (uint64_t)P.nests * P.nschemes * P.nsteps;
+
+  for (int t = 0; t < P.nsteps; ++t) {
+    for (int b = tid; b < nb; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    const uint64_t f0 = (uint64_t)t * ss, f1 = f0 + ss;
+    int bad = 0;
+    for (uint64_t f = f0 + tid; f < f1; f += blockDim.x) {
+      unsigned v = row[f];
+      if (v >= (unsigned)nb) bad = 1;
+      else atomicAdd(&hist[v], 1u);
+    }
+    if (bad) badrange = 1;
+    __syncthreads();
+    for (int b = tid; b < nb; b += blockDim.x) cum[b] += hist[b];
+    __syncthreads();
+    if (freq_out)
+      for (int b = tid; b < nb; b += blockDim.x)
+        freq_out[((uint64_t)dof * P.nsteps + t) * nsum + off + b] = cum[b];
+    // L sum for the 2-D factorisation (deterministic order, one thread)
+    if (tid == 0) {
+      double L = 0.0;
+      if (P.jacobian && hj)
+        for (int b = 0; b < nb; ++b)
+          if (cum[b]) L += (double)cum[b] * log(type == 1 ? mids[b] * mids[b] : sin(mids[b]));
+      lsum[((uint64_t)dof * P.nschemes + s) * P.nsteps + t] = L;
+    }
+    // entropies: one warp per estimator
+    const int e = tid >> 5, lane = tid & 31;
+    if (e < P.nests) {
+      const int est = P.ests[e];
+      const double nd = (t + 1.0) * (double)ss;
+      double acc = 0.0;
+      if (est == 0 || est == 1) {
+        int blank = 0;
+        for (int b = lane; b < nb; b += 32) {
+          double fq = (double)cum[b] / nd;
+          double pd = fq / w;
+          if (pd > 0.0) {
+            if (P.jacobian && hj) {
+              double jf = (type == 1) ? pow(mids[b], 2) : sin(mids[b]);
+              pd = pd / jf;
+              acc += jf * pd * log(pd);
+            } else {
+              acc += pd * log(pd);
+            }
+          }
+          blank += (cum[b] == 0);
+        }
+        for (int o = 16; o; o >>= 1) {
+          acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          blank += __shfl_xor_sync(0xffffffffu, blank, o);
+        }
+        acc *= -w;
+        if (est == 1) acc += ((nb - blank) - 1) / (2.0 * nd);
+      } else if (est == 2) {  // Chao-Shen (src/Estimators.cpp:285-345)
+        int single = 0;
+        for (int b = lane; b < nb; b += 32) single += (cum[b] == 1);
+        for (int o = 16; o; o >>= 1) single += __shfl_xor_sync(0xffffffffu, single, o);
+        const double g = 1 - ((uint8_t)single / nd);
+        for (int b = lane; b < nb; b += 32) {
+          double fq = g * ((double)cum[b] / nd);
+          double pd = fq / w;
+          if (pd > 0.0) {
+            double den = 1 - pow((1 - fq), nd);
+            if (P.jacobian && hj) {
+              double jf = (type == 1) ? pow(mids[b], 2) : sin(mids[b]);
+              pd = pd / jf;
+              acc += jf * pd * log(pd) / den;
+            } else {
+              acc += pd * log(pd) / den;
+            }
+          }
+        }
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        acc *= -w;
+      } else {  // James-Stein (src/Estimators.cpp:298-316)
+        const double tk = 1.0 / (double)nb;
+        double s2 = 0, t2 = 0;
+        for (int b = lane; b < nb; b += 32) {
+          double fq = (double)cum[b] / nd;
+          s2 += fq * fq;
+          t2 += (tk - fq) * (tk - fq);
+        }
+        for (int o = 16; o; o >>= 1) {
+          s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+          t2 += __shfl_xor_sync(0xffffffffu, t2, o);
+        }
+        const double lam = (1 - s2) / ((nd - 1) * t2);
+        for (int b = lane; b < nb; b += 32) {
+          double fq = (lam * tk) + ((1 - lam) * ((double)cum[b] / nd));
+          double pd = fq / w;
+          if (pd > 0.0) {
+            if (P.jacobian && hj) {
+              double jf = (type == 1) ? pow(mids[b], 2) : sin(mids[b]);
+              pd = pd / jf;
+              acc += jf * pd * log(pd);
+            } else {
+              acc += pd * log(pd);
+            }
+          }
+        }
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        acc *= -w;
+      }
+      if (lane == 0) s1[(uint64_t)dof * per + ((uint64_t)e * P.nschemes + s) * P.nsteps + t] = acc;
+    }
+    __syncthreads();
+  }
+  if (badrange && tid == 0) atomicOr(flag, kFlagBinRange);
+}
+
+// ----------------------------------------------------------------------------
+// Shared-memory atomic joint histograms ("plain" count form).
+//
+// A task is a small tile of rows x cols DOFs whose pairs share a CTA; each
+// pair owns an nb*nb uint32 histogram in shared memory.  Threads walk the
+// frames of a step four at a time (one 32-bit load per DOF), increment the
+// pair histograms with shared-memory atomics, and at every step boundary the
+// CTA reduces each histogram to (sum round(c ln c 2^32), non-empty cells) or,
+// in counts mode, writes the cumulative histograms out.
+__device__ __forceinline__ uint64_t tri_index(uint64_t i, uint64_t j, uint64_t n) {
+  // row-major index of pair (i, j), i < j, among all pairs of n items
+  return i * n - i * (i + 1) / 2 + (j - i - 1);
+}
+
+template <bool kCounts>
+__global__ void __launch_bounds__(512)
+pairs_atomic_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__ tasks,
+                    const __grid_constant__ PairParams P,
+                    const unsigned long long *__restrict__ clnc_tab,
+                    unsigned long long *__restrict__ sclnc, unsigned *__restrict__ nnz,
+                    unsigned *__restrict__ counts, int *__restrict__ flag) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  unsigned *hist = reinterpret_cast<unsigned *>(dyn);
+  __shared__ unsigned long long tab[kTabSmem];
+  __shared__ uint32_t rows[16], cols[16];
+  __shared__ uint64_t outidx[16];
+  __shared__ int nr_s, nc_s, np_s, badflag;
+  const int tid = threadIdx.x;
+  const int nb = P.nb, nb2 = nb * nb;
+  const uint64_t n = P.nframes;
+
+  if (tid == 0) {
+    badflag = 0;
+    if (P.all_pairs) {
+      // implicit upper-triangular task grid over R x R tiles
+      const uint64_t T = P.ntile;
+      uint64_t id = blockIdx.x, bi = 0;
+      // invert id = bi*T - bi*(bi-1)/2 + (bj - bi)
+      while (true) {
+        uint64_t rowlen = T - bi;
+        if (id < rowlen) break;
+        id -= rowlen;
+        ++bi;
+      }
+      const uint64_t bj = bi + id;
+      int nr = 0, nc = 0, np = 0;
+      for (int r = 0; r < P.tile; ++r)
+        if (bi * P.tile + r < P.ndof) rows[nr++] = (uint32_t)(bi * P.tile + r);
+      for (int c = 0; c < P.tile; ++c)
+        if (bj * P.tile + c < P.ndof) cols[nc++] = (uint32_t)(bj * P.tile + c);
+      for (int r = 0; r < nr; ++r)
+        for (int c = 0; c < nc; ++c) {
+          uint32_t i = rows[r], j = cols[c];
+          outidx[r * nc + c] = (i < j) ? tri_index(i, j, P.ndof) : ~0ull;
+          ++np;
+        }
+      nr_s = nr;
+      nc_s = nc;
+      np_s = nr * nc;
+    } else {
+      const PairTask &tk = tasks[blockIdx.x];
+      for (int r = 0; r < tk.nr; ++r) rows[r] = tk.rows[r];
+      for (int c = 0; c < tk.nc; ++c) cols[c] = tk.cols[c];
+      for (int q = 0; q < tk.nr * tk.nc; ++q) outidx[q] = tk.out[q];
+      nr_s = tk.nr;
+      nc_s = tk.nc;
+      np_s = tk.nr * tk.nc;
+    }
+  }
+  for (int i = tid; i < kTabSmem; i += blockDim.x) tab[i] = clnc_tab[i];
+  __syncthreads();
+  const int nr = nr_s, nc = nc_s, np = np_s;
+  for (int i = tid; i < np * nb2; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+
+  const uint8_t *rp[4], *cp[16];
+  for (int r = 0; r < nr; ++r) rp[r] = bins + ((uint64_t)rows[r] * P.nschemes + P.scheme) * n;
+  for (int c = 0; c < nc; ++c) cp[c] = bins + ((uint64_t)cols[c] * P.nschemes + P.scheme) * n;
+  const bool word = (n & 3) == 0;
+  int bad = 0;
+
+  for (int t = 0; t < P.nsteps; ++t) {
+    const uint64_t f0 = (uint64_t)t * P.step_size, f1 = f0 + P.step_size;
+    if (word) {
+      const uint64_t g0 = f0 >> 2, g1 = (f1 + 3) >> 2;
+      for (uint64_t g = g0 + tid; g < g1; g += blockDim.x) {
+        const uint64_t fb = g << 2;
+        unsigned rv[4], cv[16];
+        for (int r = 0; r < nr; ++r) rv[r] = __ldg(reinterpret_cast<const unsigned *>(rp[r]) + g);
+        for (int c = 0; c < nc; ++c) cv[c] = __ldg(reinterpret_cast<const unsigned *>(cp[c]) + g);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const uint64_t f = fb + q;
+          if (f < f0 || f >= f1) continue;
+          for (int r = 0; r < nr; ++r) {
+            const unsigned a = (rv[r] >> (8 * q)) & 255u;
+            for (int c = 0; c < nc; ++c) {
+              const unsigned b = (cv[c] >> (8 * q)) & 255u;
+              if (a < (unsigned)nb && b < (unsigned)nb)
+                atomicAdd(&hist[(r * nc + c) * nb2 + a * nb + b], 1u);
+              else
+                bad = 1;
+            }
+          }
+        }
+      }
+    } else {
+      for (uint64_t f = f0 + tid; f < f1; f += blockDim.x) {
+        for (int r = 0; r < nr; ++r) {
+          const unsigned a = rp[r][f];
+          for (int c = 0; c < nc; ++c) {
+            const unsigned b = cp[c][f];
+            if (a < (unsigned)nb && b < (unsigned)nb)
+              atomicAdd(&hist[(r * nc + c) * nb2 + a * nb + b], 1u);
+            else
+              bad = 1;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (kCounts) {
+      for (int q = 0; q < np; ++q) {
+        const uint64_t o = outidx[q];
+        if (o == ~0ull) continue;
+        unsigned *dst = counts + (o * P.nsteps + t) * (uint64_t)nb2;
+        for (int i = tid; i < nb2; i += blockDim.x) dst[i] = hist[q * nb2 + i];
+      }
+    } else {
+      // one warp per pair: sum_c round(c ln c 2^32) and non-empty cells
+      const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
+      for (int q = warp; q < np; q += nwarps) {
+        const uint64_t o = outidx[q];
+        if (o == ~0ull) continue;
+        unsigned long long acc = 0;
+        unsigned cntnz = 0;
+        const unsigned *h = hist + q * nb2;
+        for (int i = lane; i < nb2; i += 32) {
+          const unsigned c = h[i];
+          acc += (c < (unsigned)kTabSmem) ? tab[c] : clnc_fixed(c);
+          cntnz += (c != 0);
+        }
+        for (int off = 16; off; off >>= 1) {
+          acc += __shfl_xor_sync(0xffffffffu, acc, off);
+          cntnz += __shfl_xor_sync(0xffffffffu, cntnz, off);
+        }
+        if (lane == 0) {
+          sclnc[o * P.nsteps + t] = acc;
+          nnz[o * P.nsteps + t] = cntnz;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (__syncthreads_or(bad) && tid == 0) atomicOr(flag, kFlagBinRange);
+}
+
+// ----------------------------------------------------------------------------
+// S2 from the integer moments (ML, MM).  One thread per (pair, step) of a
+// scheme.
+__global__ void finalize2d_kernel(const uint32_t *__restrict__ pairs, int all_pairs,
+                                  uint32_t ndof, const double *__restrict__ ext,
+                                  const double *__restrict__ lsum,
+                                  const unsigned long long *__restrict__ sclnc,
+                                  const unsigned *__restrict__ nnz,
+                                  const __grid_constant__ EntParams P, int scheme,
+                                  uint64_t npairs, double *__restrict__ s2) {
+  const uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (idx >= npairs * P.nsteps) return;
+  const uint64_t p = idx / P.nsteps;
+  const int t = (int)(idx % P.nsteps);
+  uint32_t i, j;
+  if (all_pairs) {
+    // invert the row-major upper-triangular index
+    const double nn = (double)ndof;
+    uint64_t r = (uint64_t)floor(((2 * nn - 1) - sqrt((2 * nn - 1) * (2 * nn - 1) - 8.0 * (double)p)) / 2);
+    while (r > 0 && r * ndof - r * (r + 1) / 2 > p) --r;
+    while ((r + 1) * ndof - (r + 1) * (r + 2) / 2 <= p) ++r;
+    i = (uint32_t)r;
+    j = (uint32_t)(p - (r * ndof - r * (r + 1) / 2) + r + 1);
+  } else {
+    i = pairs[2 * p];
+    j = pairs[2 * p + 1];
+  }
+  const int nb = P.schemes[scheme];
+  double w1 = __ddiv_rn(__dsub_rn(ext[4 * i + 1], ext[4 * i]), (double)nb);
+  double w2 = __ddiv_rn(__dsub_rn(ext[4 * j + 1], ext[4 * j]), (double)nb);
+  if (P.kde) w1 = w2 = 1.0;
+  const double nd = (t + 1.0) * (double)P.step_size;
+  const double X = (double)sclnc[idx] * kClncInvScale;
+  const double L = lsum[((uint64_t)i * P.nschemes + scheme) * P.nsteps + t] +
+                   lsum[((uint64_t)j * P.nschemes + scheme) * P.nsteps + t];
+  const double S = log(nd) + log(w1 * w2) + (L - X) / nd;
+  const uint64_t per = (uint64_t)P.nests * P.nschemes * P.nsteps;
+  for (int e = 0; e < P.nests; ++e) {
+    double v = S;
+    if (P.ests[e] == 1) v += ((double)nnz[idx] - 1.0) / (2.0 * nd);
+    s2[p * per + ((uint64_t)e * P.nschemes + scheme) * P.nsteps + t] = v;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Per-cell entropy2D on materialised counts (every estimator), one CTA per
+// pair.  Mirrors src/Estimators.cpp:455-645 including the Chao-Shen branch's
+// use of the row bin centre for the second DOF's Jacobian (:555-566).
+__global__ void __launch_bounds__(256)
+entropy2d_counts_kernel(const uint32_t *__restrict__ pairs, const uint8_t *__restrict__ types,
+                        const double *__restrict__ ext, const unsigned *__restrict__ counts,
+                        const __grid_constant__ EntParams P, int scheme, uint64_t p0,
+                        uint64_t npairs, double *__restrict__ s2) {
+  const uint64_t p = p0 + blockIdx.x;
+  if (p >= npairs) return;
+  const uint32_t i = pairs[2 * p], j = pairs[2 * p + 1];
+  const int nb = P.schemes[scheme];
+  const unsigned nb2 = (unsigned)nb * nb;
+  const int t1 = types[i], t2 = types[j];
+  const bool hj1 = (t1 == 1 || t1 == 2), hj2 = (t2 == 1 || t2 == 2);
+  double w1 = __ddiv_rn(__dsub_rn(ext[4 * i + 1], ext[4 * i]), (double)nb);
+  double w2 = __ddiv_rn(__dsub_rn(ext[4 * j + 1], ext[4 * j]), (double)nb);
+  const double hw1 = w1 / 2, hw2 = w2 / 2;
+  if (P.kde) w1 = w2 = 1.0;
+  __shared__ double mid1[256], mid2[256], red[32];
+  __shared__ unsigned long long redu[32];
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    mid1[b] = hj1 ? __dadd_rn(__dadd_rn(ext[4 * i], __dmul_rn((double)b, w1)), hw1) : 0.0;
+    mid2[b] = hj2 ? __dadd_rn(__dadd_rn(ext[4 * j], __dmul_rn((double)b, w2)), hw2) : 0.0;
+  }
+  __syncthreads();
+  const double area = w1 * w2;
+  const uint64_t per = (uint64_t)P.nests * P.nschemes * P.nsteps;
+  auto jac = [](int type, double m) { return type == 1 ? pow(m, 2) : sin(m); };
+  auto bsum_d = [&](double v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+    return s;
+  };
+  auto bsum_u = [&](unsigned long long v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) redu[threadIdx.x >> 5] = v;
+    __syncthreads();
+    unsigned long long s = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += redu[q];
+    return s;
+  };
+  for (int t = 0; t < P.nsteps; ++t) {
+    const unsigned *c = counts + ((p - p0) * P.nsteps + t) * (uint64_t)nb2;
+    const double nd = (t + 1.0) * (double)P.step_size;
+    for (int e = 0; e < P.nests; ++e) {
+      const int est = P.ests[e];
+      double g = 1.0, lam = 0.0;
+      const double tk = 1.0 / (double)nb;
+      unsigned long long blank = 0;
+      if (est == 1) {
+        unsigned long long z = 0;
+        for (unsigned q = threadIdx.x; q < nb2; q += blockDim.x) z += (c[q] == 0);
+        blank = bsum_u(z);
+      } else if (est == 2) {
+        unsigned long long z = 0;
+        for (unsigned q = threadIdx.x; q < nb2; q += blockDim.x) z += (c[q] == 1);
+        unsigned single = (unsigned)bsum_u(z);
+        g = 1 - (single / nd);
+      } else if (est == 3) {
+        double a = 0, b = 0;
+        for (unsigned q = threadIdx.x; q < nb2; q += blockDim.x) {
+          double f = c[q] / nd;
+          a += f * f;
+          b += (tk - f) * (tk - f);
+        }
+        a = bsum_d(a);
+        b = bsum_d(b);
+        lam = (1 - a) / ((nd - 1) * b);
+      }
+      double acc = 0.0;
+      for (unsigned q = threadIdx.x; q < nb2; q += blockDim.x) {
+        const int jj = q / nb, kk = q % nb;
+        double f = c[q] / nd;
+        if (est == 2) f = g * (c[q] / nd);
+        if (est == 3) f = (lam * tk) + ((1 - lam) * f);
+        double pd = f / area;
+        if (pd > 0.0) {
+          const double jf1 = hj1 ? jac(t1, mid1[jj]) : 1.0;
+          double jf2 = 1.0;
+          if (hj2) jf2 = jac(t2, est == 2 ? mid2[jj] : mid2[kk]);
+          double den = (est == 2) ? 1 - pow((1 - f), nd) : 1.0;
+          if (P.jacobian) {
+            const double jf = jf1 * jf2;
+            pd = pd / jf;
+            acc += jf * pd * log(pd) / den;
+          } else {
+            acc += pd * log(pd) / den;
+          }
+        }
+      }
+      acc = bsum_d(acc) * -area;
+      if (est == 1) acc += ((nb2 - (unsigned)blank) - 1) / (2.0 * nd);
+      if (threadIdx.x == 0) s2[p * per + ((uint64_t)e * P.nschemes + scheme) * P.nsteps + t] = acc;
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+int init_clnc_table(centre_ctx *ctx, unsigned long long *tab) {
+  clnc_table_kernel<<<(kTabGlobal + 255) / 256, 256, 0, ctx->stream>>>(tab, kTabGlobal);
+  ctx->launches++;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  return CENTRE_OK;
+}
+
+int launch_entropy1d(centre_ctx *ctx, const EntParams &P, uint32_t ndof, const uint8_t *d_types,
+                     const uint8_t *d_bins, const double *d_ext, double *d_s1,
+                     unsigned long long *d_freq, double *d_lsum) {
+  if (ndof == 0) return CENTRE_OK;
+  KernelTimer kt(ctx, CENTRE_TIMER_COUNTS1D);
+  entropy1d_kernel<<<ndof * P.nschemes, 256, 0, ctx->stream>>>(d_bins, d_types, d_ext, P, d_s1,
+                                                               d_freq, d_lsum, ctx->d_flag);
+  ctx->launches++;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  return CENTRE_OK;
+}
+
+int pair_tile_for(int nb) {
+  // pairs whose nb*nb uint32 histograms fit the shared-memory budget
+  const size_t budget = 192 * 1024;
+  const size_t per = (size_t)nb * nb * 4;
+  int p = (int)std::min<size_t>(16, budget / per);
+  return p;
+}
+
+int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
+                        uint64_t ntasks, const unsigned long long *d_tab,
+                        unsigned long long *d_sclnc, unsigned *d_nnz, unsigned *d_counts) {
+  if (ntasks == 0) return CENTRE_OK;
+  const int ppair = P.all_pairs ? P.tile * P.tile : std::max(1, std::min(16, pair_tile_for(P.nb)));
+  KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
+  size_t smem = (size_t)ppair * P.nb * P.nb * 4;
+  if (d_counts) {
+    CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_atomic_kernel<true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pairs_atomic_kernel<true><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
+        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+  } else {
+    CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_atomic_kernel<false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pairs_atomic_kernel<false><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
+        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+  }
+  ctx->launches++;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  return CENTRE_OK;
+}
+
+int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uint32_t *d_pairs,
+                      int all_pairs, uint32_t ndof, const double *d_ext, const double *d_lsum,
+                      const unsigned long long *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
+                      double *d_s2) {
+  const uint64_t total = npairs * P.nsteps;
+  if (total == 0) return CENTRE_OK;
+  finalize2d_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(
+      d_pairs, all_pairs, ndof, d_ext, d_lsum, d_sclnc, d_nnz, P, scheme, npairs, d_s2);
+  ctx->launches++;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  return CENTRE_OK;
+}
+
+int launch_entropy2d_counts(centre_ctx *ctx, const EntParams &P, int scheme,
+                            const uint32_t *d_pairs, const uint8_t *d_types, const double *d_ext,
+                            const unsigned *d_counts, uint64_t p0, uint64_t np, uint64_t npairs,
+                            double *d_s2) {
+  if (np == 0) return CENTRE_OK;
+  entropy2d_counts_kernel<<<(unsigned)np, 256, 0, ctx->stream>>>(d_pairs, d_types, d_ext,
+                                                                  d_counts, P, scheme, p0, npairs,
+                                                                  d_s2);
+  ctx->launches++;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  return CENTRE_OK;
+}
+
+}  // namespace centre

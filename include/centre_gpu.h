@@ -1,0 +1,200 @@
+/*
+ * centre_gpu.h -- C ABI of the GB300 (sm_103a) CENTRE entropy hot path.
+ *
+ * The reference (shaileshp51/centre) has no plugin or FFI layer: its hot path
+ * is three C++ stage classes (Discretizer, EntropyCalculator, EntropyScorer)
+ * over free numeric functions.  Each entry point below replaces one of those
+ * functions or stage loops; the reference file:line it stands in for is given
+ * beside it.  Signatures use plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Every call returns a centre_status (0 = success, < 0 = error) and never
+ *    exits the process; centre_gpu_strerror() names the code and
+ *    centre_gpu_last_error() gives a message for the last failing call.
+ *  - Functions without a suffix take HOST pointers and block until their
+ *    results are back in host memory.  The *_dev variants take DEVICE pointers
+ *    and are enqueued on the context's stream (centre_gpu_set_stream) without
+ *    synchronising.
+ *  - One context per host thread; a context is not thread-safe.
+ *  - Layouts are the reference's:
+ *      BAT input   [ndof][nframes] float32, DOF-major (Netcdf_BAT.cpp:236-330
+ *                  transposes the file's [frame][dof] into this)
+ *      bins        [ndof][nschemes][nframes] uint8 (Netcdf_TrjInt coord var)
+ *      extremes    [ndof][4] float64: min, max, avg, phase
+ *      entropies   [ndof or npairs][nestimators][nschemes][nsteps] float64
+ *                  (Netcdf_EntContri contri_S, Estimators.cpp:239-243)
+ *      pairs       [npairs][2] uint32 DOF indices into the bins array
+ */
+#ifndef CENTRE_GPU_H
+#define CENTRE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CENTRE_GPU_ABI_VERSION 1
+
+typedef struct centre_ctx centre_ctx;
+
+typedef enum centre_status {
+  CENTRE_OK = 0,
+  CENTRE_E_ARG = -1,          /* invalid argument                           */
+  CENTRE_E_CUDA = -2,         /* CUDA runtime error                         */
+  CENTRE_E_NOMEM = -3,        /* device allocation failed                   */
+  CENTRE_E_BINRANGE = -4,     /* a bin index >= its scheme's bin count      */
+  CENTRE_E_TIMEOUT = -5,      /* a device-side wait ran out its limit       */
+  CENTRE_E_UNSUPPORTED = -6,  /* combination not supported on this path     */
+  CENTRE_E_NODEVICE = -7      /* no usable sm_103 device                    */
+} centre_status;
+
+/* BAT_t, src/Centre.h:42-47 */
+enum { CENTRE_NONE = 0, CENTRE_BOND = 1, CENTRE_ANGLE = 2, CENTRE_DIHEDRAL = 3 };
+/* EntropyEstimators, src/Centre.h:89-94 */
+enum { CENTRE_ML = 0, CENTRE_MM = 1, CENTRE_CS = 2, CENTRE_JS = 3 };
+/* How the 2-D joint counts are formed. */
+enum {
+  CENTRE_COUNTS_AUTO = 0,   /* one-hot tensor-core form where it applies  */
+  CENTRE_COUNTS_ATOMIC = 1, /* shared-memory atomic histograms            */
+  CENTRE_COUNTS_TC = 2      /* FP8 one-hot O^T O on tcgen05 tensor cores  */
+};
+
+/* Entropy-stage parameters ([entropy]/[control]/[histogram] keys of the
+ * reference input file, src/Inputs.cpp:100-553). */
+typedef struct centre_entropy_params {
+  uint64_t nframes;           /* frames per DOF in the bins array           */
+  uint8_t nsteps;             /* [control] nsteps                           */
+  uint8_t nschemes;           /* number of bin schemes                      */
+  uint8_t nestimators;        /* number of estimators                       */
+  uint8_t jacobian;           /* [entropy] jacobian                         */
+  uint8_t kde;                /* pdfmethod == vonmiseskde                   */
+  uint8_t counts_form;        /* CENTRE_COUNTS_*                            */
+  uint8_t bin_schemes[16];    /* [histogram] nbins (first nschemes used)    */
+  uint8_t estimators[4];      /* [entropy] estimator (first nestimators)    */
+} centre_entropy_params;
+
+/* ------------------------------------------------------------ context ---- */
+int centre_gpu_create(centre_ctx **ctx, int device);
+void centre_gpu_destroy(centre_ctx *ctx);
+const char *centre_gpu_strerror(int status);
+const char *centre_gpu_last_error(const centre_ctx *ctx);
+int centre_gpu_set_stream(centre_ctx *ctx, void *cuda_stream);
+int centre_gpu_synchronize(centre_ctx *ctx);
+/* Number of kernels this library has launched on the context so far. */
+uint64_t centre_gpu_launch_count(const centre_ctx *ctx);
+
+/* Device time of the library's hot kernels, measured with CUDA events on the
+ * context's stream while timing is enabled (no reference counterpart: the
+ * reference's ProgState timers, src/main_common.h:52-163, time whole
+ * stages on the host).  centre_gpu_timer synchronises the stream and
+ * returns the milliseconds and launch count accumulated since timing was
+ * enabled for one class. */
+enum {
+  CENTRE_TIMER_DISCRETIZE = 0, /* histogram discretisation kernel      */
+  CENTRE_TIMER_COUNTS1D = 1,   /* 1-D counts / entropies kernel        */
+  CENTRE_TIMER_PAIRS = 2,      /* 2-D joint count kernel (either form) */
+  CENTRE_TIMER_SCORE = 3,      /* MI, sums and spanning-tree kernels   */
+  CENTRE_TIMER_CLASSES = 4
+};
+int centre_gpu_enable_timing(centre_ctx *ctx, int enable);
+int centre_gpu_timer(centre_ctx *ctx, int which, double *ms, uint64_t *launches);
+
+/* ----------------------------------------------------- discretisation ---- */
+/* Histogram binning of one DOF-type block: Real2Int::bndReal2Int
+ * (src/Real2Int.cpp:27), ::angReal2Int (:131), ::dihReal2Int (:244), driven
+ * per DOF as in Discretizer::run_dtype (src/Discretizer.cpp:138-207).
+ * bins_ref and optimize_dih are [histogram] referencenbins and
+ * [discretization] optimizedih.  Bin indices and min/max/phase are
+ * bit-identical to the reference; avg agrees to rounding. */
+int centre_gpu_discretize(centre_ctx *ctx, int bat_type, const float *data,
+                          uint32_t ndof, uint64_t nframes,
+                          const uint8_t *bin_schemes, uint32_t nschemes,
+                          uint8_t bins_ref, int optimize_dih, uint8_t *bins,
+                          double *extremes);
+int centre_gpu_discretize_dev(centre_ctx *ctx, int bat_type, const float *data,
+                              uint32_t ndof, uint64_t nframes,
+                              const uint8_t *bin_schemes, uint32_t nschemes,
+                              uint8_t bins_ref, int optimize_dih,
+                              uint8_t *bins, double *extremes);
+
+/* von Mises KDE conformer assignment of torsions: Real2Int::getMinimaPositions
+ * (src/Real2Int.cpp:481) with analyticGrad=false as Discretizer.cpp:177 calls
+ * it.  minima [ndof][nmaxconf] radians, nfound [ndof]. */
+int centre_gpu_discretize_vmkde(centre_ctx *ctx, const float *data,
+                                uint32_t ndof, uint64_t nframes,
+                                uint8_t nmaxconf, double kappa,
+                                uint32_t sdo_nstep, double sdo_conv,
+                                uint32_t sdo_niter, uint8_t *bins,
+                                double *minima, uint8_t *nfound);
+
+/* ------------------------------------------------------------ entropy ---- */
+/* 1-D counts and entropies: binData1D (src/Estimators.cpp:56) + entropy1D
+ * (:217) for every DOF, as EntropyCalculator::run1d (EntropyCalculator.cpp:
+ * 156-199).  s1 [ndof][nest][nsch][nsteps]; freq (optional, may be NULL)
+ * [ndof][nsteps][sum nb] cumulative counts. */
+int centre_gpu_entropy1d(centre_ctx *ctx, const centre_entropy_params *p,
+                         uint32_t ndof, const uint8_t *types,
+                         const uint8_t *bins, const double *extremes,
+                         double *s1, uint64_t *freq);
+int centre_gpu_entropy1d_dev(centre_ctx *ctx, const centre_entropy_params *p,
+                             uint32_t ndof, const uint8_t *types,
+                             const uint8_t *bins, const double *extremes,
+                             double *s1, uint64_t *freq);
+
+/* 2-D joint entropies of a pair list: binData2D (src/Estimators.cpp:130) +
+ * entropy2D (:391) per pair, as EntropyCalculator::run2d_xx/run2d_xy
+ * (EntropyCalculator.cpp:281, :674).  pairs == NULL means every pair i<j of
+ * the ndof DOFs in row-major order.  s2 [npairs][nest][nsch][nsteps]. */
+int centre_gpu_entropy2d(centre_ctx *ctx, const centre_entropy_params *p,
+                         uint32_t ndof, const uint8_t *types,
+                         const uint8_t *bins, const double *extremes,
+                         uint64_t npairs, const uint32_t *pairs, double *s2);
+int centre_gpu_entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p,
+                             uint32_t ndof, const uint8_t *types,
+                             const uint8_t *bins, const double *extremes,
+                             uint64_t npairs, const uint32_t *pairs,
+                             double *s2);
+
+/* Joint counts only, for parity checks of the count kernels: binData2D
+ * (src/Estimators.cpp:130-205) per pair.  freq [npairs][nsteps][sum nb^2]
+ * cumulative, cell a*nb+b. */
+int centre_gpu_counts2d(centre_ctx *ctx, const centre_entropy_params *p,
+                        uint32_t ndof, const uint8_t *bins, uint64_t npairs,
+                        const uint32_t *pairs, uint64_t *freq);
+
+/* ------------------------------------------------------------ scoring ---- */
+/* Number of doubles per (estimator, scheme, step) in the sums outputs: the
+ * columns of the reference's MIE/MIST convergence CSV after TIME
+ * (EntropyScorer.cpp:574-629): BOND-S1 ANGLE-S1 DIHED-S1, then S2 and I2 for
+ * B/B A/A D/D B/A B/D A/D, then S1 and S2 totals. */
+#define CENTRE_SUMS_COLS 17
+
+/* EntropyScorer::run (src/EntropyScorer.cpp:287-866): MI = S_i + S_j - S_ij
+ * (getMaxMI2D, src/Convergance.cpp:183-194), MIE sums, and when build_tree is
+ * non-zero the MIST maximum spanning tree (boruvkaMST, src/Centre.cpp:5) over
+ * the pair list in the given order (edge order breaks ties: the first edge
+ * of largest MI wins, as in the reference).  DOF types give the B/A/D
+ * blocks.
+ *   mi        [npairs][nest][nsch][nsteps] (may be NULL)
+ *   mie_sums  [nest][nsch][nsteps][CENTRE_SUMS_COLS]
+ *   mist_sums [nest][nsch][nsteps][CENTRE_SUMS_COLS] (build_tree only)
+ *   tree      [nest][nsch][nsteps][ndof-1] pair indices, sorted by MI desc
+ *             then index (build_tree only); ntree [nest][nsch][nsteps]. */
+int centre_gpu_score(centre_ctx *ctx, const centre_entropy_params *p,
+                     uint32_t ndof, const uint8_t *types, const double *s1,
+                     uint64_t npairs, const uint32_t *pairs, const double *s2,
+                     int build_tree, double *mi, double *mie_sums,
+                     double *mist_sums, uint32_t *tree, uint32_t *ntree);
+int centre_gpu_score_dev(centre_ctx *ctx, const centre_entropy_params *p,
+                         uint32_t ndof, const uint8_t *types, const double *s1,
+                         uint64_t npairs, const uint32_t *pairs,
+                         const double *s2, int build_tree, double *mi,
+                         double *mie_sums, double *mist_sums, uint32_t *tree,
+                         uint32_t *ntree);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CENTRE_GPU_H */

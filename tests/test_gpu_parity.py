@@ -1,0 +1,276 @@
+"""GPU parity: the CUDA library through its C ABI against the CPU oracle and
+the reference's golden fixtures.  Bins and counts must be bit-identical;
+entropies agree within 1e-9 relative (the reference's own tolerance for this
+path), MI within 1e-9 absolute."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from centre_gb300.api import CentreError, make_params
+from centre_gb300.synth import chain_trajectory
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-9
+
+
+def all_pairs(n):
+    return np.array([(i, j) for i in range(n) for j in range(i + 1, n)], np.uint32).reshape(-1, 2)
+
+
+def stack_blocks(tr, gpu, schemes, optimize=True):
+    bins, ext, types = [], [], []
+    for typ, blk in tr.blocks():
+        b, e = gpu.discretize(typ, blk, schemes, bins_ref=schemes[0], optimize=optimize)
+        bins.append(b)
+        ext.append(e)
+        types += [typ] * len(b)
+    return np.concatenate(bins), np.concatenate(ext), np.array(types, np.uint8)
+
+
+# ------------------------------------------------------------ discretise --
+def test_discretize_golden_fixture(gpu, golden):
+    g = golden("discretize_ref.npz")
+    for sch_name, sch in (("s30", [30]), ("s2", [50, 7])):
+        for typ, name in ((1, "bonds"), (2, "angles"), (3, "torsions")):
+            for opt in ((1, 0) if typ == 3 else (1,)):
+                bins, ext = gpu.discretize(typ, g[name], sch, bins_ref=sch[0], optimize=bool(opt))
+                key = f"{name}_{sch_name}_o{opt}"
+                assert np.array_equal(bins, g[key + "_bins"]), key
+                want = g[key + "_ext"]
+                assert np.array_equal(ext[:, [0, 1, 3]], want[:, [0, 1, 3]]), key
+                np.testing.assert_allclose(ext[:, 2], want[:, 2], rtol=1e-12, err_msg=key)
+
+
+@pytest.mark.parametrize("nframes", [50_000, 20_001, 1_003, 37, 150_000])
+def test_discretize_synthetic_vs_oracle(gpu, orc, nframes):
+    tr = chain_trajectory(9, nframes, seed=nframes)
+    for typ, blk in tr.blocks():
+        for sch in ([30], [50, 7, 255]):
+            for opt in ((True, False) if typ == 3 else (True,)):
+                gb, ge = gpu.discretize(typ, blk, sch, bins_ref=sch[0], optimize=opt)
+                ob, oe = orc.discretize(typ, blk, sch, bins_ref=sch[0], optimize=opt)
+                assert np.array_equal(gb, ob), (typ, sch, opt)
+                assert np.array_equal(ge[:, [0, 1, 3]], oe[:, [0, 1, 3]])
+                np.testing.assert_allclose(ge[:, 2], oe[:, 2], rtol=1e-12)
+
+
+def test_discretize_rejects_out_of_domain(gpu):
+    x = np.full((2, 64), 1.0, np.float32)
+    x[1, 5] = 7.0   # torsion >= 2pi
+    with pytest.raises(CentreError) as e:
+        gpu.discretize(3, x, [10])
+    assert e.value.status == -1
+    x = np.full((1, 64), 1.5, np.float32)
+    x[0, 3] = -0.1  # negative bond
+    with pytest.raises(CentreError):
+        gpu.discretize(1, x, [10])
+    x = np.full((1, 64), 1.5, np.float32)
+    x[0, 3] = np.nan
+    with pytest.raises(CentreError):
+        gpu.discretize(2, x, [10])
+
+
+# ----------------------------------------------------------------- 1-D ----
+def test_entropy1d_golden_fixture(gpu, golden):
+    g = golden("entropy_ref.npz")
+    sch = g["schemes"].tolist()
+    for jac in (0, 1):
+        p = make_params(g["bins"].shape[2], int(g["nsteps"]), sch, g["ests"].tolist(), bool(jac))
+        s1 = gpu.entropy1d(p, g["types"], g["bins"], g["ext"])
+        np.testing.assert_allclose(s1, g[f"s1_j{jac}"], rtol=RTOL, atol=1e-12)
+    p = make_params(4000, int(g["nsteps"]), [3], g["ests"].tolist(), True, kde=True)
+    s1 = gpu.entropy1d(p, np.full(4, 3, np.uint8), g["kde_bins"], np.full((4, 4), 1000.0))
+    np.testing.assert_allclose(s1, g["kde_s1"], rtol=RTOL, atol=1e-12)
+
+
+def test_entropy1d_counts_exact(gpu, orc):
+    tr = chain_trajectory(8, 30_011, seed=5)
+    bins, ext, types = stack_blocks(tr, gpu, [30, 11])
+    p = make_params(bins.shape[2], 7, [30, 11], [0, 1, 2, 3], True)
+    s1, freq = gpu.entropy1d(p, types, bins, ext, want_freq=True)
+    for d in range(len(bins)):
+        want = orc.bin1d(bins[d], 7, [30, 11])
+        assert np.array_equal(freq[d].reshape(-1), want)
+    o = orc.entropy1d(types, bins, ext, 7, [30, 11], [0, 1, 2, 3], True)
+    np.testing.assert_allclose(s1, o, rtol=RTOL, atol=1e-12)
+
+
+# ----------------------------------------------------------------- 2-D ----
+@pytest.mark.parametrize("nframes,nsteps", [(20_000, 4), (10_007, 3), (4_096, 1)])
+def test_counts2d_exact(gpu, orc, nframes, nsteps):
+    tr = chain_trajectory(6, nframes, seed=nframes + nsteps)
+    bins, ext, types = stack_blocks(tr, gpu, [30, 7])
+    pairs = all_pairs(len(bins))
+    p = make_params(nframes, nsteps, [30, 7])
+    freq = gpu.counts2d(p, bins, pairs)
+    for q, (i, j) in enumerate(pairs):
+        want = orc.bin2d(bins[i], bins[j], nsteps, [30, 7])
+        assert np.array_equal(freq[q].reshape(-1), want), (i, j)
+
+
+def test_entropy2d_golden_fixture(gpu, golden):
+    g = golden("entropy_ref.npz")
+    sch = g["schemes"].tolist()
+    for jac in (0, 1):
+        p = make_params(g["bins"].shape[2], int(g["nsteps"]), sch, g["ests"].tolist(), bool(jac),
+                        counts_form=1)
+        s2 = gpu.entropy2d(p, g["types"], g["bins"], g["ext"], g["pairs"])
+        np.testing.assert_allclose(s2, g[f"s2_j{jac}"], rtol=RTOL, atol=1e-12)
+    kp = all_pairs(4)
+    p = make_params(4000, int(g["nsteps"]), [3], g["ests"].tolist(), True, kde=True, counts_form=1)
+    s2 = gpu.entropy2d(p, np.full(4, 3, np.uint8), g["kde_bins"], np.full((4, 4), 1000.0), kp)
+    np.testing.assert_allclose(s2, g["kde_s2"], rtol=RTOL, atol=1e-12)
+
+
+@pytest.mark.parametrize("ests", [[0], [0, 1], [1]])
+def test_entropy2d_moments_all_pairs_vs_oracle(gpu, orc, ests):
+    tr = chain_trajectory(12, 40_000, seed=len(ests))
+    bins, ext, types = stack_blocks(tr, gpu, [50])
+    p = make_params(40_000, 10, [50], ests, True, counts_form=1)
+    s2 = gpu.entropy2d(p, types, bins, ext)       # all pairs, implicit
+    pairs = all_pairs(len(bins))
+    o = orc.entropy2d(pairs, types, bins, ext, 10, [50], ests, True)
+    np.testing.assert_allclose(s2, o, rtol=RTOL, atol=1e-12)
+    s2b = gpu.entropy2d(p, types, bins, ext, pairs)  # explicit list
+    assert np.array_equal(s2, s2b)
+
+
+def test_entropy2d_explicit_pair_list_orientation(gpu, orc):
+    tr = chain_trajectory(10, 12_000, seed=3)
+    bins, ext, types = stack_blocks(tr, gpu, [20])
+    rng = np.random.default_rng(0)
+    pairs = rng.integers(0, len(bins), size=(60, 2)).astype(np.uint32)
+    pairs = pairs[pairs[:, 0] != pairs[:, 1]]
+    for ests in ([0, 1], [2, 3], [0, 1, 2, 3]):
+        p = make_params(12_000, 4, [20], ests, True, counts_form=1)
+        s2 = gpu.entropy2d(p, types, bins, ext, pairs)
+        o = orc.entropy2d(pairs, types, bins, ext, 4, [20], ests, True)
+        np.testing.assert_allclose(s2, o, rtol=RTOL, atol=1e-12)
+
+
+def test_entropy2d_rejects_bad_bins(gpu):
+    bins = np.zeros((3, 1, 1000), np.uint8)
+    bins[1, 0, 10] = 40
+    ext = np.tile(np.array([0.0, 1.0, 0.5, 0.0]), (3, 1))
+    p = make_params(1000, 2, [30], [0], True, counts_form=1)
+    with pytest.raises(CentreError) as e:
+        gpu.entropy2d(p, np.array([1, 1, 1], np.uint8), bins, ext)
+    assert e.value.status == -4
+
+
+# --------------------------------------------------------------- score ----
+def reference_edge_order(types):
+    """Pairs in the reference's edge-list order: B/B, B/A, B/D, A/A, A/D, D/D
+    blocks, row-major within each (src/EntropyScorer.cpp:675-741)."""
+    idx = {t: np.nonzero(types == t)[0] for t in (1, 2, 3)}
+    out = []
+    for a, b in ((1, 1), (1, 2), (1, 3), (2, 2), (2, 3), (3, 3)):
+        for x in idx[a]:
+            for y in idx[b]:
+                if a != b or x < y:
+                    out.append((x, y))
+    return np.array(out, np.uint32)
+
+
+def test_score_sums_and_tree_vs_oracle(gpu, orc):
+    tr = chain_trajectory(14, 30_000, seed=9)
+    bins, ext, types = stack_blocks(tr, gpu, [30])
+    p = make_params(30_000, 5, [30], [0, 1], True, counts_form=1)
+    s1 = gpu.entropy1d(p, types, bins, ext)
+    pairs = reference_edge_order(types)
+    s2 = gpu.entropy2d(p, types, bins, ext, pairs)
+    out = gpu.score(p, types, s1, s2, pairs)
+    G = 2 * 1 * 5
+    mi = out["mi"].reshape(len(pairs), G)
+    s1g = s1.reshape(len(types), G)
+    np.testing.assert_allclose(mi, s1g[pairs[:, 0]] + s1g[pairs[:, 1]] - s2.reshape(len(pairs), G),
+                               rtol=0, atol=1e-12)
+    mie = out["mie"].reshape(G, 17)
+    blocks = {(1, 1): 3, (2, 2): 5, (3, 3): 7, (1, 2): 9, (1, 3): 11, (2, 3): 13}
+    tp = np.sort(types[pairs], axis=1)
+    for g in range(G):
+        for t in (1, 2, 3):
+            np.testing.assert_allclose(mie[g, t - 1], s1g[types == t, g].sum(), rtol=1e-12)
+        for (a, b), col in blocks.items():
+            m = (tp[:, 0] == a) & (tp[:, 1] == b)
+            np.testing.assert_allclose(mie[g, col], s2.reshape(len(pairs), G)[m, g].sum(), rtol=1e-12)
+            np.testing.assert_allclose(mie[g, col + 1], mi[m, g].sum(), rtol=1e-9, atol=1e-9)
+        # tree: the reference's Boruvka on the same edge order
+        t_or = orc.mst(len(types), pairs[:, 0], pairs[:, 1], mi[:, g])
+        assert sorted(out["tree"][g].tolist()) == sorted(t_or.tolist())
+        mist = out["mist"].reshape(G, 17)[g]
+        np.testing.assert_allclose(mist[16], mie[g, 15] - mi[t_or, g].sum(), rtol=1e-9, atol=1e-9)
+    # implicit all-pairs mode ranks edges in the same reference order
+    s2u = gpu.entropy2d(p, types, bins, ext)
+    outu = gpu.score(p, types, s1, s2u)
+    ap = all_pairs(len(types))
+    for g in range(G):
+        got = {tuple(ap[q]) for q in outu["tree"][g]}
+        want = {tuple(pairs[q]) for q in out["tree"][g]}
+        assert got == want
+
+
+def test_score_tree_ties_follow_reference_order(gpu, orc, golden):
+    g = golden("mst_ref.npz")
+    for k in range(12):
+        nv = int(g[f"g{k}_nv"])
+        src, dst, w = g[f"g{k}_src"], g[f"g{k}_dst"], g[f"g{k}_w"]
+        # feed MI through the scorer: s1 = 0, s2 = -w  =>  MI = w
+        p = make_params(4, 1, [2], [0], False)
+        types = np.full(nv, 3, np.uint8)
+        s1 = np.zeros((nv, 1, 1, 1))
+        s2 = (-w).reshape(-1, 1, 1, 1)
+        pairs = np.stack([src, dst], 1)
+        out = gpu.score(p, types, s1, s2, pairs)
+        got = sorted((int(src[q]), int(dst[q])) for q in out["tree"][0])
+        want = sorted(zip(g[f"g{k}_tsrc"].tolist(), g[f"g{k}_tdst"].tolist()))
+        assert got == want, k
+
+
+# ----------------------------------------------------------- example-1 ----
+def test_example1_on_gpu(gpu):
+    d = np.load(os.path.join(GOLDEN, "example1.npz"))
+    with open(os.path.join(GOLDEN, "example1.json")) as f:
+        meta = json.load(f)
+    names = {"B": "bonds", "A": "angles", "T": "torsions"}
+    tcode = {"B": 1, "A": 2, "T": 3}
+    coord = np.concatenate([d[f"{names[k]}_coord"] for k in "BAT"])
+    ext = np.concatenate([d[f"{names[k]}_ext"] for k in "BAT"])
+    types = np.concatenate([np.full(len(d[f"{names[k]}_coord"]), tcode[k], np.uint8) for k in "BAT"])
+    off = {"B": 0, "A": len(d["bonds_coord"]), "T": len(d["bonds_coord"]) + len(d["angles_coord"])}
+    p = make_params(coord.shape[2], 4, [30], [0], True)
+    s1 = gpu.entropy1d(p, types, coord, ext)
+    col = meta["mie_columns"].index("DIHED-S1")
+    for step in range(4):
+        assert abs(s1[types == 3, 0, 0, step].sum() - meta["mie_rows"][step][col]) <= 0.5e-4 + 1e-9
+    s2 = gpu.entropy2d(p, types, coord, ext)
+    ap = all_pairs(len(types))
+    lut = {tuple(x): q for q, x in enumerate(ap.tolist())}
+    for step in range(4):
+        for a, b, i, j, want in meta["trees"][str(step)]:
+            x, y = off[a] + i, off[b] + j
+            q = lut[(min(x, y), max(x, y))]
+            mi = s1[x, 0, 0, step] + s1[y, 0, 0, step] - s2[q, 0, 0, step]
+            assert abs(mi - want) <= 0.5e-6 + 1e-9
+
+
+# ------------------------------------------------- size-independent checks --
+def test_full_size_properties(gpu):
+    """At the 1000-atom shape: counts cover every frame of every step,
+    plug-in MI is non-negative, results are run-to-run identical."""
+    import torch
+    tr = chain_trajectory(60, 100_000, seed=1, coupling="block8")
+    bins, ext, types = stack_blocks(tr, gpu, [50])
+    p = make_params(100_000, 10, [50], [0, 1], True, counts_form=1)
+    s1, freq = gpu.entropy1d(p, types, bins, ext, want_freq=True)
+    assert np.all(freq.sum(axis=2) == (np.arange(1, 11) * 10_000)[None, :])
+    s2 = gpu.entropy2d(p, types, bins, ext)
+    s2b = gpu.entropy2d(p, types, bins, ext)
+    assert np.array_equal(s2, s2b)
+    out = gpu.score(p, types, s1, s2, build_tree=False)
+    assert out["mi"][:, 0].min() > -1e-10   # ML plug-in MI >= 0
+    del torch
