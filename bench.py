@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "MI pairs/s"
 UNIT = "pairs/s"
-NBINS = 50
+NBINS = 50      # set from the workload in main()
 NSTEPS = 10
 
 
@@ -411,6 +411,9 @@ def main():
     ap.add_argument("--no-compare-atomic", dest="compare_atomic", action="store_false")
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     args = ap.parse_args()
+    global NBINS, NSTEPS
+    w = workload(args.workload)
+    NBINS, NSTEPS = w["nbins"], w["nsteps"]
     if args.impl == "reference":
         run_reference(args)
     else:

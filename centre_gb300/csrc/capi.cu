@@ -187,8 +187,8 @@ int counts_chunk(centre_ctx *ctx, const EntParams &E, int scheme, uint32_t ndof,
   P.nb = nb;
   P.nsteps = E.nsteps;
   P.all_pairs = 0;
-  CENTRE_TRY(launch_pairs_atomic(ctx, P, d_tasks, tasks.size(), ctx_clnc(ctx), nullptr, nullptr,
-                                 d_counts));
+  CENTRE_TRY(launch_pairs_atomic(ctx, P, d_tasks, tasks.size(), (const U128 *)ctx_clnc(ctx),
+                                 nullptr, nullptr, d_counts));
   // the task buffer is reused by the next chunk: finish this one first
   CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return CENTRE_OK;
@@ -207,7 +207,7 @@ std::vector<uint32_t> all_pairs_list(uint32_t ndof) {
 
 }  // namespace
 
-unsigned long long *ctx_clnc(centre_ctx *ctx) { return ctx->d_clnc; }
+void *ctx_clnc(centre_ctx *ctx) { return ctx->d_clnc; }
 
 // ---------------------------------------------------------------------------
 int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof,
@@ -234,9 +234,10 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
     if (!d_tmp) return st;
     double *d_lsum = d_tmp + (uint64_t)ndof * per;
     CENTRE_TRY(launch_entropy1d(ctx, E, ndof, d_types, d_bins, d_ext, d_tmp, nullptr, d_lsum));
-    unsigned long long *d_sclnc = (unsigned long long *)scratch(
-        ctx, kSlotMoments, (sizeof(unsigned long long) + sizeof(unsigned)) * npairs * E.nsteps, &st);
+    U128 *d_sclnc = (U128 *)scratch(ctx, kSlotMoments,
+                                    (sizeof(U128) + sizeof(unsigned)) * npairs * E.nsteps, &st);
     if (!d_sclnc) return st;
+    const U128 *d_tab = (const U128 *)ctx->d_clnc;
     unsigned *d_nnz = reinterpret_cast<unsigned *>(d_sclnc + npairs * E.nsteps);
     std::vector<uint32_t> h_pairs;
     for (int s = 0; s < E.nschemes; ++s) {
@@ -258,7 +259,7 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
                          "tensor-core counts need the all-pairs form and a supported bin count");
       if (use_tc) {
         P.all_pairs = 1;
-        CENTRE_TRY(launch_pairs_tc(ctx, P, ctx->d_clnc, d_sclnc, d_nnz));
+        CENTRE_TRY(launch_pairs_tc(ctx, P, d_tab, d_sclnc, d_nnz));
       } else {
         if ((size_t)nb * nb * 4 > 200 * 1024)
           return set_error(ctx, CENTRE_E_UNSUPPORTED, "bin count too large for shared-memory counts");
@@ -270,7 +271,7 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
           P.tile = tile;
           P.ntile = (ndof + tile - 1) / tile;
           const uint64_t ntasks = P.ntile * (P.ntile + 1) / 2;
-          CENTRE_TRY(launch_pairs_atomic(ctx, P, nullptr, ntasks, ctx->d_clnc, d_sclnc, d_nnz,
+          CENTRE_TRY(launch_pairs_atomic(ctx, P, nullptr, ntasks, d_tab, d_sclnc, d_nnz,
                                          nullptr));
         } else {
           if (h_pairs.empty()) {
@@ -288,7 +289,7 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
           if (!d_tasks) return st;
           CENTRE_CUDA(ctx, cudaMemcpyAsync(d_tasks, tasks.data(), sizeof(PairTask) * tasks.size(),
                                            cudaMemcpyHostToDevice, ctx->stream));
-          CENTRE_TRY(launch_pairs_atomic(ctx, P, d_tasks, tasks.size(), ctx->d_clnc, d_sclnc,
+          CENTRE_TRY(launch_pairs_atomic(ctx, P, d_tasks, tasks.size(), d_tab, d_sclnc,
                                          d_nnz, nullptr));
           CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         }
@@ -378,14 +379,13 @@ int centre_gpu_create(centre_ctx **out, int device) {
                        "stream")) != CENTRE_OK ||
       (rc = check_cuda(ctx, cudaMalloc(&ctx->d_flag, sizeof(int)), "flag")) != CENTRE_OK ||
       (rc = check_cuda(ctx, cudaMallocHost(&ctx->h_flag, sizeof(int)), "flag")) != CENTRE_OK ||
-      (rc = check_cuda(ctx, cudaMalloc(&ctx->d_clnc, sizeof(unsigned long long) * kTabGlobal),
+      (rc = check_cuda(ctx, cudaMalloc(&ctx->d_clnc, sizeof(U128) * kTabGlobal),
                        "table")) != CENTRE_OK) {
     centre_gpu_destroy(ctx);
     return rc;
   }
   ctx->own_stream = true;
-  unsigned long long *tab = ctx->d_clnc;
-  rc = init_clnc_table(ctx, tab);
+  rc = init_clnc_table(ctx, (U128 *)ctx->d_clnc);
   if (rc == CENTRE_OK) rc = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "init");
   if (rc != CENTRE_OK) {
     centre_gpu_destroy(ctx);

@@ -17,12 +17,8 @@ constexpr int kMaxBins = 255;
 constexpr int kMaxSchemes = 16;
 constexpr int kMaxSteps = 255;
 
-// Fixed-point scale of the per-cell c*ln(c) terms: sums of round(c ln c *
-// 2^32) are exact integers, so the joint-entropy sums are identical however
-// the cells are distributed over threads, tiles or count kernels.  With
-// counts <= 2^27 the per-step sum (<= n ln n * 2^32) fits in uint64.
-constexpr double kClncScale = 4294967296.0;
-constexpr double kClncInvScale = 1.0 / 4294967296.0;
+// Largest frame count: counts stay below 2^27, so a per-pair sum of up to
+// 65025 cells of c ln c * 2^60 fits in 128 bits.
 constexpr uint64_t kMaxFrames = 1ull << 27;
 
 // Grow-only device scratch owned by a context.
@@ -44,7 +40,7 @@ struct centre_ctx {
   int *d_flag = nullptr;   // device error flag (bin range, timeouts)
   int *h_flag = nullptr;   // pinned mirror
   int cc_major = 0, cc_minor = 0;
-  unsigned long long *d_clnc = nullptr;  // round(c ln c 2^32), c < 2^16
+  void *d_clnc = nullptr;  // c ln c as 128-bit fixed point, c < 2^16
   // event timing of the hot kernels (centre_gpu_enable_timing)
   bool timing = false;
   struct TimerRec {
@@ -74,7 +70,7 @@ enum ScratchSlot {
 int set_error(centre_ctx *ctx, int status, const std::string &msg);
 int check_cuda(centre_ctx *ctx, cudaError_t e, const char *what);
 void *scratch(centre_ctx *ctx, int slot, size_t bytes, int *status);
-unsigned long long *ctx_clnc(centre_ctx *ctx);
+void *ctx_clnc(centre_ctx *ctx);
 
 // Scoped event timer around a launch on the context's stream (no-op unless
 // timing is enabled).

@@ -29,7 +29,7 @@ namespace centre {
 
 // ----------------------------------------------------------------------------
 // c*ln(c) fixed-point table
-__global__ void clnc_table_kernel(unsigned long long *t, int n) {
+__global__ void clnc_table_kernel(U128 *t, int n) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n) t[c] = clnc_fixed((unsigned)c);
 }
@@ -194,12 +194,12 @@ template <bool kCounts>
 __global__ void __launch_bounds__(512)
 pairs_atomic_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__ tasks,
                     const __grid_constant__ PairParams P,
-                    const unsigned long long *__restrict__ clnc_tab,
-                    unsigned long long *__restrict__ sclnc, unsigned *__restrict__ nnz,
+                    const U128 *__restrict__ clnc_tab, U128 *__restrict__ sclnc,
+                    unsigned *__restrict__ nnz,
                     unsigned *__restrict__ counts, int *__restrict__ flag) {
   extern __shared__ __align__(16) unsigned char dyn[];
   unsigned *hist = reinterpret_cast<unsigned *>(dyn);
-  __shared__ unsigned long long tab[kTabSmem];
+  __shared__ U128 tab[kTabSmem];
   __shared__ uint32_t rows[16], cols[16];
   __shared__ uint64_t outidx[16];
   __shared__ int nr_s, nc_s, np_s, badflag;
@@ -310,16 +310,17 @@ pairs_atomic_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict
       for (int q = warp; q < np; q += nwarps) {
         const uint64_t o = outidx[q];
         if (o == ~0ull) continue;
-        unsigned long long acc = 0;
+        U128 acc;
+        acc.lo = acc.hi = 0ull;
         unsigned cntnz = 0;
         const unsigned *h = hist + q * nb2;
         for (int i = lane; i < nb2; i += 32) {
           const unsigned c = h[i];
-          acc += (c < (unsigned)kTabSmem) ? tab[c] : clnc_fixed(c);
+          acc = u128_add(acc, (c < (unsigned)kTabSmem) ? tab[c] : clnc_fixed(c));
           cntnz += (c != 0);
         }
         for (int off = 16; off; off >>= 1) {
-          acc += __shfl_xor_sync(0xffffffffu, acc, off);
+          acc = u128_add(acc, u128_shfl_xor(acc, off));
           cntnz += __shfl_xor_sync(0xffffffffu, cntnz, off);
         }
         if (lane == 0) {
@@ -339,7 +340,7 @@ pairs_atomic_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict
 __global__ void finalize2d_kernel(const uint32_t *__restrict__ pairs, int all_pairs,
                                   uint32_t ndof, const double *__restrict__ ext,
                                   const double *__restrict__ lsum,
-                                  const unsigned long long *__restrict__ sclnc,
+                                  const U128 *__restrict__ sclnc,
                                   const unsigned *__restrict__ nnz,
                                   const __grid_constant__ EntParams P, int scheme,
                                   uint64_t npairs, double *__restrict__ s2) {
@@ -365,7 +366,7 @@ __global__ void finalize2d_kernel(const uint32_t *__restrict__ pairs, int all_pa
   double w2 = __ddiv_rn(__dsub_rn(ext[4 * j + 1], ext[4 * j]), (double)nb);
   if (P.kde) w1 = w2 = 1.0;
   const double nd = (t + 1.0) * (double)P.step_size;
-  const double X = (double)sclnc[idx] * kClncInvScale;
+  const double X = u128_value(sclnc[idx]);
   const double L = lsum[((uint64_t)i * P.nschemes + scheme) * P.nsteps + t] +
                    lsum[((uint64_t)j * P.nschemes + scheme) * P.nsteps + t];
   const double S = log(nd) + log(w1 * w2) + (L - X) / nd;
@@ -482,7 +483,7 @@ entropy2d_counts_kernel(const uint32_t *__restrict__ pairs, const uint8_t *__res
 }
 
 // ----------------------------------------------------------------------------
-int init_clnc_table(centre_ctx *ctx, unsigned long long *tab) {
+int init_clnc_table(centre_ctx *ctx, U128 *tab) {
   clnc_table_kernel<<<(kTabGlobal + 255) / 256, 256, 0, ctx->stream>>>(tab, kTabGlobal);
   ctx->launches++;
   CENTRE_CUDA(ctx, cudaGetLastError());
@@ -510,8 +511,8 @@ int pair_tile_for(int nb) {
 }
 
 int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
-                        uint64_t ntasks, const unsigned long long *d_tab,
-                        unsigned long long *d_sclnc, unsigned *d_nnz, unsigned *d_counts) {
+                        uint64_t ntasks, const U128 *d_tab, U128 *d_sclnc, unsigned *d_nnz,
+                        unsigned *d_counts) {
   if (ntasks == 0) return CENTRE_OK;
   const int ppair = P.all_pairs ? P.tile * P.tile : std::max(1, std::min(16, pair_tile_for(P.nb)));
   KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
@@ -534,7 +535,7 @@ int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_
 
 int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uint32_t *d_pairs,
                       int all_pairs, uint32_t ndof, const double *d_ext, const double *d_lsum,
-                      const unsigned long long *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
+                      const U128 *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
                       double *d_s2) {
   const uint64_t total = npairs * P.nsteps;
   if (total == 0) return CENTRE_OK;

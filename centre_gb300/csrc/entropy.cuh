@@ -48,25 +48,65 @@ struct PairParams {
 constexpr int kTabSmem = 1024;      // c ln c entries kept in shared memory
 constexpr int kTabGlobal = 1 << 16; // entries in the global table
 
-// round(c ln c * 2^32); exact integer sums of these give the joint-entropy
-// cell sum independent of summation order.
-__device__ __forceinline__ unsigned long long clnc_fixed(unsigned c) {
-  if (c < 2) return 0ull;
-  const double v = (double)c * log((double)c) * kClncScale;
-  return __double2ull_rn(v);
+// Unsigned 128-bit accumulator for the per-cell c ln c terms.
+struct __align__(16) U128 {
+  unsigned long long lo, hi;
+};
+
+__device__ __forceinline__ U128 u128_add(U128 a, U128 b) {
+  U128 r;
+  asm("add.cc.u64 %0, %2, %4;\n\taddc.u64 %1, %3, %5;"
+      : "=l"(r.lo), "=l"(r.hi)
+      : "l"(a.lo), "l"(a.hi), "l"(b.lo), "l"(b.hi));
+  return r;
 }
 
-int init_clnc_table(centre_ctx *ctx, unsigned long long *tab);
+__device__ __forceinline__ U128 u128_shfl_xor(U128 v, int o) {
+  v.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+  v.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+  return v;
+}
+
+// The double c*log(c) represented exactly as an integer multiple of 2^-60:
+// its 53-bit significand shifted by its exponent (c >= 2 gives an exponent
+// >= 0, so the shift is a left shift of at least 8 and nothing is rounded).
+// Integer sums of these are the exact sums of the per-cell doubles, so the
+// cell sum is independent of how cells are spread over threads, tiles or
+// count kernels.
+__device__ __forceinline__ U128 clnc_fixed(unsigned c) {
+  U128 r;
+  r.lo = 0ull;
+  r.hi = 0ull;
+  if (c < 2) return r;
+  const double v = (double)c * log((double)c);
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+  const unsigned long long m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int s = e + 8;  // value = m * 2^(e - 52 + 60)
+  if (s >= 64) {
+    r.hi = m << (s - 64);
+  } else {
+    r.lo = m << s;
+    r.hi = m >> (64 - s);
+  }
+  return r;
+}
+
+__host__ __device__ __forceinline__ double u128_value(U128 x) {
+  return (double)x.hi * 16.0 + (double)x.lo * 0x1p-60;
+}
+
+int init_clnc_table(centre_ctx *ctx, U128 *tab);
 int launch_entropy1d(centre_ctx *ctx, const EntParams &P, uint32_t ndof, const uint8_t *d_types,
                      const uint8_t *d_bins, const double *d_ext, double *d_s1,
                      unsigned long long *d_freq, double *d_lsum);
 int pair_tile_for(int nb);
 int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
-                        uint64_t ntasks, const unsigned long long *d_tab,
-                        unsigned long long *d_sclnc, unsigned *d_nnz, unsigned *d_counts);
+                        uint64_t ntasks, const U128 *d_tab, U128 *d_sclnc, unsigned *d_nnz,
+                        unsigned *d_counts);
 int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uint32_t *d_pairs,
                       int all_pairs, uint32_t ndof, const double *d_ext, const double *d_lsum,
-                      const unsigned long long *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
+                      const U128 *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
                       double *d_s2);
 int launch_entropy2d_counts(centre_ctx *ctx, const EntParams &P, int scheme,
                             const uint32_t *d_pairs, const uint8_t *d_types, const double *d_ext,
@@ -80,8 +120,8 @@ int launch_discretize(centre_ctx *ctx, int bat_type, const float *d_data, uint32
 
 // pairs_tc.cu
 bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes);
-int launch_pairs_tc(centre_ctx *ctx, const PairParams &P, const unsigned long long *d_tab,
-                    unsigned long long *d_sclnc, unsigned *d_nnz);
+int launch_pairs_tc(centre_ctx *ctx, const PairParams &P, const U128 *d_tab, U128 *d_sclnc,
+                    unsigned *d_nnz);
 
 // score.cu
 struct ScoreParams {

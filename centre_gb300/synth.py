@@ -93,6 +93,7 @@ def chain_trajectory(natoms: int, nframes: int, seed: int = 0,
 # Named workloads (chain size, frames, bins, steps, coupling).
 WORKLOADS = {
     "chain25": dict(natoms=25, nframes=50_000, nbins=30, nsteps=4, coupling="neighbour"),
+    "chain200": dict(natoms=200, nframes=100_000, nbins=50, nsteps=10, coupling="block8"),
     "chain1000": dict(natoms=1000, nframes=100_000, nbins=50, nsteps=10, coupling="block8"),
     "chain5000": dict(natoms=5000, nframes=100_000, nbins=50, nsteps=10, coupling="block8"),
 }

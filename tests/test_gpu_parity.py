@@ -1,7 +1,8 @@
 """GPU parity: the CUDA library through its C ABI against the CPU oracle and
 the reference's golden fixtures.  Bins and counts must be bit-identical;
-entropies agree within 1e-9 relative (the reference's own tolerance for this
-path), MI within 1e-9 absolute."""
+entropies agree within 1e-9 relative, with an absolute floor of 1e-13 for
+entropies within rounding of zero (different summation orders of the
+reference's own per-cell sum already differ at ~1e-15 absolute)."""
 import json
 import os
 
@@ -81,10 +82,10 @@ def test_entropy1d_golden_fixture(gpu, golden):
     for jac in (0, 1):
         p = make_params(g["bins"].shape[2], int(g["nsteps"]), sch, g["ests"].tolist(), bool(jac))
         s1 = gpu.entropy1d(p, g["types"], g["bins"], g["ext"])
-        np.testing.assert_allclose(s1, g[f"s1_j{jac}"], rtol=RTOL, atol=1e-12)
+        np.testing.assert_allclose(s1, g[f"s1_j{jac}"], rtol=RTOL, atol=1e-13)
     p = make_params(4000, int(g["nsteps"]), [3], g["ests"].tolist(), True, kde=True)
     s1 = gpu.entropy1d(p, np.full(4, 3, np.uint8), g["kde_bins"], np.full((4, 4), 1000.0))
-    np.testing.assert_allclose(s1, g["kde_s1"], rtol=RTOL, atol=1e-12)
+    np.testing.assert_allclose(s1, g["kde_s1"], rtol=RTOL, atol=1e-13)
 
 
 def test_entropy1d_counts_exact(gpu, orc):
@@ -96,7 +97,7 @@ def test_entropy1d_counts_exact(gpu, orc):
         want = orc.bin1d(bins[d], 7, [30, 11])
         assert np.array_equal(freq[d].reshape(-1), want)
     o = orc.entropy1d(types, bins, ext, 7, [30, 11], [0, 1, 2, 3], True)
-    np.testing.assert_allclose(s1, o, rtol=RTOL, atol=1e-12)
+    np.testing.assert_allclose(s1, o, rtol=RTOL, atol=1e-13)
 
 
 # ----------------------------------------------------------------- 2-D ----
@@ -119,11 +120,11 @@ def test_entropy2d_golden_fixture(gpu, golden):
         p = make_params(g["bins"].shape[2], int(g["nsteps"]), sch, g["ests"].tolist(), bool(jac),
                         counts_form=1)
         s2 = gpu.entropy2d(p, g["types"], g["bins"], g["ext"], g["pairs"])
-        np.testing.assert_allclose(s2, g[f"s2_j{jac}"], rtol=RTOL, atol=1e-12)
+        np.testing.assert_allclose(s2, g[f"s2_j{jac}"], rtol=RTOL, atol=1e-13)
     kp = all_pairs(4)
     p = make_params(4000, int(g["nsteps"]), [3], g["ests"].tolist(), True, kde=True, counts_form=1)
     s2 = gpu.entropy2d(p, np.full(4, 3, np.uint8), g["kde_bins"], np.full((4, 4), 1000.0), kp)
-    np.testing.assert_allclose(s2, g["kde_s2"], rtol=RTOL, atol=1e-12)
+    np.testing.assert_allclose(s2, g["kde_s2"], rtol=RTOL, atol=1e-13)
 
 
 @pytest.mark.parametrize("ests", [[0], [0, 1], [1]])
@@ -134,7 +135,7 @@ def test_entropy2d_moments_all_pairs_vs_oracle(gpu, orc, ests):
     s2 = gpu.entropy2d(p, types, bins, ext)       # all pairs, implicit
     pairs = all_pairs(len(bins))
     o = orc.entropy2d(pairs, types, bins, ext, 10, [50], ests, True)
-    np.testing.assert_allclose(s2, o, rtol=RTOL, atol=1e-12)
+    np.testing.assert_allclose(s2, o, rtol=RTOL, atol=1e-13)
     s2b = gpu.entropy2d(p, types, bins, ext, pairs)  # explicit list
     assert np.array_equal(s2, s2b)
 
@@ -149,7 +150,7 @@ def test_entropy2d_explicit_pair_list_orientation(gpu, orc):
         p = make_params(12_000, 4, [20], ests, True, counts_form=1)
         s2 = gpu.entropy2d(p, types, bins, ext, pairs)
         o = orc.entropy2d(pairs, types, bins, ext, 4, [20], ests, True)
-        np.testing.assert_allclose(s2, o, rtol=RTOL, atol=1e-12)
+        np.testing.assert_allclose(s2, o, rtol=RTOL, atol=1e-13)
 
 
 def test_entropy2d_rejects_bad_bins(gpu):
@@ -188,7 +189,7 @@ def test_score_sums_and_tree_vs_oracle(gpu, orc):
     mi = out["mi"].reshape(len(pairs), G)
     s1g = s1.reshape(len(types), G)
     np.testing.assert_allclose(mi, s1g[pairs[:, 0]] + s1g[pairs[:, 1]] - s2.reshape(len(pairs), G),
-                               rtol=0, atol=1e-12)
+                               rtol=0, atol=1e-13)
     mie = out["mie"].reshape(G, 17)
     blocks = {(1, 1): 3, (2, 2): 5, (3, 3): 7, (1, 2): 9, (1, 3): 11, (2, 3): 13}
     tp = np.sort(types[pairs], axis=1)
