@@ -138,6 +138,18 @@ class Context:
                                               len(pairs), _ptr(pairs), _ptr(freq)))
         return freq
 
+    def pair_moments(self, params: EntropyParams, bins, scheme=0):
+        """Integer moments of every pair i<j: (clnc [npairs][nsteps][2] uint64
+        as (low, high) words of sum c ln c * 2^60, nnz [npairs][nsteps])."""
+        bins = _c(bins, np.uint8)
+        ndof = bins.shape[0]
+        npairs = ndof * (ndof - 1) // 2
+        clnc = np.zeros((npairs, params.nsteps, 2), np.uint64)
+        nnz = np.zeros((npairs, params.nsteps), np.uint32)
+        self.check(self.L.centre_gpu_pair_moments(self.h, C.byref(params), ndof, _ptr(bins),
+                                                  int(scheme), _ptr(clnc), _ptr(nnz)))
+        return clnc, nnz
+
     def score(self, params: EntropyParams, types, s1, s2, pairs=None, build_tree=True,
               want_mi=True, mi_out=None):
         types = _c(types, np.uint8)

@@ -625,6 +625,59 @@ int centre_gpu_counts2d(centre_ctx *ctx, const centre_entropy_params *p, uint32_
   return CENTRE_OK;
 }
 
+int centre_gpu_pair_moments(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof,
+                            const uint8_t *bins, int scheme, uint64_t *clnc, uint32_t *nnz) {
+  if (!ctx || !p || !bins || !clnc || !nnz) return set_error(ctx, CENTRE_E_ARG, "null argument");
+  cudaSetDevice(ctx->device);
+  EntParams E;
+  CENTRE_TRY(validate_params(ctx, p, &E));
+  if (scheme < 0 || scheme >= E.nschemes) return set_error(ctx, CENTRE_E_ARG, "bad scheme");
+  if (ndof < 2) return CENTRE_OK;
+  const uint64_t npairs = (uint64_t)ndof * (ndof - 1) / 2;
+  int st = CENTRE_OK;
+  const size_t nbb = (size_t)ndof * E.nschemes * E.nframes;
+  unsigned char *d_in = (unsigned char *)scratch(ctx, kSlotIn, nbb, &st);
+  if (!d_in) return st;
+  U128 *d_m = (U128 *)scratch(ctx, kSlotMoments, (sizeof(U128) + 4) * npairs * E.nsteps, &st);
+  if (!d_m) return st;
+  unsigned *d_z = reinterpret_cast<unsigned *>(d_m + npairs * E.nsteps);
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(d_in, bins, nbb, cudaMemcpyHostToDevice, ctx->stream));
+  CENTRE_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+  PairParams P;
+  memset(&P, 0, sizeof(P));
+  P.bins = d_in;
+  P.nframes = E.nframes;
+  P.step_size = E.step_size;
+  P.ndof = ndof;
+  P.nschemes = E.nschemes;
+  P.scheme = scheme;
+  P.nb = E.schemes[scheme];
+  P.nsteps = E.nsteps;
+  P.all_pairs = 1;
+  if (p->counts_form == CENTRE_COUNTS_TC) {
+    if (!tc_supported(ctx, P.nb, E.nframes))
+      return set_error(ctx, CENTRE_E_UNSUPPORTED, "tensor-core counts not supported here");
+    CENTRE_TRY(launch_pairs_tc(ctx, P, (const U128 *)ctx->d_clnc, d_m, d_z));
+  } else {
+    if ((size_t)P.nb * P.nb * 4 > 200 * 1024)
+      return set_error(ctx, CENTRE_E_UNSUPPORTED, "bin count too large for shared-memory counts");
+    int ppair = atomic_pair_width(P.nb);
+    int tile = 1;
+    while ((tile + 1) * (tile + 1) <= ppair && tile < 4) ++tile;
+    P.tile = tile;
+    P.ntile = (ndof + tile - 1) / tile;
+    CENTRE_TRY(launch_pairs_atomic(ctx, P, nullptr, P.ntile * (P.ntile + 1) / 2,
+                                   (const U128 *)ctx->d_clnc, d_m, d_z, nullptr));
+  }
+  CENTRE_TRY(read_flag(ctx));
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(clnc, d_m, sizeof(U128) * npairs * E.nsteps,
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(nnz, d_z, 4 * npairs * E.nsteps, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+  CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return CENTRE_OK;
+}
+
 // ---- scoring ---------------------------------------------------------------
 static int score_impl(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof,
                       const uint8_t *d_types, const uint8_t *h_types, const double *d_s1,

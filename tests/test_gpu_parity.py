@@ -275,3 +275,39 @@ def test_full_size_properties(gpu):
     out = gpu.score(p, types, s1, s2, build_tree=False)
     assert out["mi"][:, 0].min() > -1e-10   # ML plug-in MI >= 0
     del torch
+
+
+# ------------------------------------------------- tensor-core counts ----
+def oracle_moments(orc, bins, nsteps, nb):
+    """sum c ln c and non-empty cells per pair/step from the oracle's counts."""
+    n = len(bins)
+    out_x, out_z = [], []
+    for i in range(n):
+        for j in range(i + 1, n):
+            f = orc.bin2d(bins[i], bins[j], nsteps, [nb]).reshape(nsteps, -1).astype(np.float64)
+            x = np.where(f > 1, f * np.log(np.where(f > 0, f, 1)), 0).sum(axis=1)
+            out_x.append(x)
+            out_z.append((f > 0).sum(axis=1))
+    return np.array(out_x), np.array(out_z)
+
+
+@pytest.mark.parametrize("natoms,nframes,nsteps,nb", [
+    (4, 4_096, 1, 50), (8, 20_000, 4, 50), (12, 10_007, 3, 30), (30, 30_000, 10, 16),
+    (10, 12_000, 2, 100), (6, 8_000, 2, 255)])
+def test_tc_counts_identical_to_atomic(gpu, orc, natoms, nframes, nsteps, nb):
+    tr = chain_trajectory(natoms, nframes, seed=natoms * 7 + nb)
+    bins, ext, types = stack_blocks(tr, gpu, [nb])
+    pa = make_params(nframes, nsteps, [nb], [0, 1], True, counts_form=1)
+    pt = make_params(nframes, nsteps, [nb], [0, 1], True, counts_form=2)
+    if nb * nb * 4 <= 200 * 1024:
+        ca, za = gpu.pair_moments(pa, bins)
+    ct, zt = gpu.pair_moments(pt, bins)
+    xo, zo = oracle_moments(orc, bins[:, 0], nsteps, nb)
+    assert np.array_equal(zt, zo)
+    xt = ct[..., 1].astype(np.float64) * 16.0 + ct[..., 0].astype(np.float64) * 2.0 ** -60
+    np.testing.assert_allclose(xt, xo, rtol=1e-12)
+    if nb * nb * 4 <= 200 * 1024:
+        assert np.array_equal(ct, ca) and np.array_equal(zt, za)
+        s_at = gpu.entropy2d(pa, types, bins, ext)
+        s_tc = gpu.entropy2d(pt, types, bins, ext)
+        assert np.array_equal(s_at, s_tc)
