@@ -157,9 +157,12 @@ void plan_tasks(const uint32_t *pairs, uint64_t p0, uint64_t p1, int width,
 }
 
 int atomic_pair_width(int nb) {
-  int w = pair_tile_for(nb);
-  return std::max(1, std::min(16, w));
+  // task widths are the kernel's instantiated column counts: 16, 8, 4, 2, 1
+  const int w = pair_tile_for(nb);
+  return w >= 16 ? 16 : w >= 8 ? 8 : w >= 4 ? 4 : w >= 2 ? 2 : 1;
 }
+
+bool atomic_fits(int nb) { return pair_tile_for(nb) >= 1; }
 
 // Counts of a chunk of an explicit pair list: [np][nsteps][nb^2] uint32.
 int counts_chunk(centre_ctx *ctx, const EntParams &E, int scheme, uint32_t ndof,
@@ -167,7 +170,7 @@ int counts_chunk(centre_ctx *ctx, const EntParams &E, int scheme, uint32_t ndof,
                  unsigned *d_counts) {
   const int nb = E.schemes[scheme];
   const int width = atomic_pair_width(nb);
-  if (width < 1 || (size_t)nb * nb * 4 > 200 * 1024)
+  if (!atomic_fits(nb))
     return set_error(ctx, CENTRE_E_UNSUPPORTED, "bin count too large for shared-memory counts");
   std::vector<PairTask> tasks;
   plan_tasks(h_pairs, p0, p1, width, tasks);
@@ -187,7 +190,7 @@ int counts_chunk(centre_ctx *ctx, const EntParams &E, int scheme, uint32_t ndof,
   P.nb = nb;
   P.nsteps = E.nsteps;
   P.all_pairs = 0;
-  CENTRE_TRY(launch_pairs_atomic(ctx, P, d_tasks, tasks.size(), (const U128 *)ctx_clnc(ctx),
+  CENTRE_TRY(launch_pairs_atomic(ctx, P, d_tasks, tasks.size(), (const double *)ctx_clnc(ctx),
                                  nullptr, nullptr, d_counts));
   // the task buffer is reused by the next chunk: finish this one first
   CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -237,7 +240,7 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
     U128 *d_sclnc = (U128 *)scratch(ctx, kSlotMoments,
                                     (sizeof(U128) + sizeof(unsigned)) * npairs * E.nsteps, &st);
     if (!d_sclnc) return st;
-    const U128 *d_tab = (const U128 *)ctx->d_clnc;
+    const double *d_tab = (const double *)ctx->d_clnc;
     unsigned *d_nnz = reinterpret_cast<unsigned *>(d_sclnc + npairs * E.nsteps);
     std::vector<uint32_t> h_pairs;
     for (int s = 0; s < E.nschemes; ++s) {
@@ -253,7 +256,12 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
       P.nb = nb;
       P.nsteps = E.nsteps;
       const int form = p->counts_form;
-      const bool use_tc = all && form != CENTRE_COUNTS_ATOMIC && tc_supported(ctx, nb, E.nframes);
+      // AUTO takes the shared-memory histogram whenever its tiles fit: at
+      // these bin counts it outruns the one-hot tensor-core contraction
+      // (B^2 multiply-adds per frame and pair against one increment); the
+      // tensor-core form covers bin counts whose histograms do not fit.
+      const bool use_tc = all && tc_supported(ctx, nb, E.nframes) &&
+                          (form == CENTRE_COUNTS_TC || (form == CENTRE_COUNTS_AUTO && !atomic_fits(nb)));
       if (form == CENTRE_COUNTS_TC && !use_tc)
         return set_error(ctx, CENTRE_E_UNSUPPORTED,
                          "tensor-core counts need the all-pairs form and a supported bin count");
@@ -261,7 +269,7 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
         P.all_pairs = 1;
         CENTRE_TRY(launch_pairs_tc(ctx, P, d_tab, d_sclnc, d_nnz));
       } else {
-        if ((size_t)nb * nb * 4 > 200 * 1024)
+        if (!atomic_fits(nb))
           return set_error(ctx, CENTRE_E_UNSUPPORTED, "bin count too large for shared-memory counts");
         if (all) {
           int ppair = atomic_pair_width(nb);
@@ -379,13 +387,13 @@ int centre_gpu_create(centre_ctx **out, int device) {
                        "stream")) != CENTRE_OK ||
       (rc = check_cuda(ctx, cudaMalloc(&ctx->d_flag, sizeof(int)), "flag")) != CENTRE_OK ||
       (rc = check_cuda(ctx, cudaMallocHost(&ctx->h_flag, sizeof(int)), "flag")) != CENTRE_OK ||
-      (rc = check_cuda(ctx, cudaMalloc(&ctx->d_clnc, sizeof(U128) * kTabGlobal),
+      (rc = check_cuda(ctx, cudaMalloc(&ctx->d_clnc, sizeof(double) * kTabGlobal),
                        "table")) != CENTRE_OK) {
     centre_gpu_destroy(ctx);
     return rc;
   }
   ctx->own_stream = true;
-  rc = init_clnc_table(ctx, (U128 *)ctx->d_clnc);
+  rc = init_clnc_table(ctx, (double *)ctx->d_clnc);
   if (rc == CENTRE_OK) rc = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "init");
   if (rc != CENTRE_OK) {
     centre_gpu_destroy(ctx);
@@ -657,9 +665,9 @@ int centre_gpu_pair_moments(centre_ctx *ctx, const centre_entropy_params *p, uin
   if (p->counts_form == CENTRE_COUNTS_TC) {
     if (!tc_supported(ctx, P.nb, E.nframes))
       return set_error(ctx, CENTRE_E_UNSUPPORTED, "tensor-core counts not supported here");
-    CENTRE_TRY(launch_pairs_tc(ctx, P, (const U128 *)ctx->d_clnc, d_m, d_z));
+    CENTRE_TRY(launch_pairs_tc(ctx, P, (const double *)ctx->d_clnc, d_m, d_z));
   } else {
-    if ((size_t)P.nb * P.nb * 4 > 200 * 1024)
+    if (!atomic_fits(P.nb))
       return set_error(ctx, CENTRE_E_UNSUPPORTED, "bin count too large for shared-memory counts");
     int ppair = atomic_pair_width(P.nb);
     int tile = 1;
@@ -667,7 +675,7 @@ int centre_gpu_pair_moments(centre_ctx *ctx, const centre_entropy_params *p, uin
     P.tile = tile;
     P.ntile = (ndof + tile - 1) / tile;
     CENTRE_TRY(launch_pairs_atomic(ctx, P, nullptr, P.ntile * (P.ntile + 1) / 2,
-                                   (const U128 *)ctx->d_clnc, d_m, d_z, nullptr));
+                                   (const double *)ctx->d_clnc, d_m, d_z, nullptr));
   }
   CENTRE_TRY(read_flag(ctx));
   CENTRE_CUDA(ctx, cudaMemcpyAsync(clnc, d_m, sizeof(U128) * npairs * E.nsteps,

@@ -40,7 +40,7 @@ struct centre_ctx {
   int *d_flag = nullptr;   // device error flag (bin range, timeouts)
   int *h_flag = nullptr;   // pinned mirror
   int cc_major = 0, cc_minor = 0;
-  void *d_clnc = nullptr;  // c ln c as 128-bit fixed point, c < 2^16
+  void *d_clnc = nullptr;  // c ln c (double) for c < 2^16
   // event timing of the hot kernels (centre_gpu_enable_timing)
   bool timing = false;
   struct TimerRec {

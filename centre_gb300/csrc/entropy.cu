@@ -29,9 +29,9 @@ namespace centre {
 
 // ----------------------------------------------------------------------------
 // c*ln(c) fixed-point table
-__global__ void clnc_table_kernel(U128 *t, int n) {
+__global__ void clnc_table_kernel(double *t, int n) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < n) t[c] = clnc_fixed((unsigned)c);
+  if (c < n) t[c] = clnc_value((unsigned)c);
 }
 
 // ----------------------------------------------------------------------------
@@ -177,155 +177,201 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
 }
 
 // ----------------------------------------------------------------------------
-// Shared-memory atomic joint histograms ("plain" count form).
+// Shared-memory atomic joint histograms.
 //
-// A task is a small tile of rows x cols DOFs whose pairs share a CTA; each
-// pair owns an nb*nb uint32 histogram in shared memory.  Threads walk the
-// frames of a step four at a time (one 32-bit load per DOF), increment the
-// pair histograms with shared-memory atomics, and at every step boundary the
-// CTA reduces each histogram to (sum round(c ln c 2^32), non-empty cells) or,
-// in counts mode, writes the cumulative histograms out.
+// A CTA owns a tile of R row DOFs x C column DOFs; each of the R*C pairs has
+// an nb*nb uint32 histogram in shared memory.  Threads walk the frames of a
+// step four at a time: one 32-bit load per DOF gives four bins, each frame's
+// R row offsets and C column offsets are formed once, and every increment is
+// one add plus one red.shared.add (about three instructions per increment).
+// Bin ranges are checked four at a time with one vector compare per word.
+// At every step boundary the CTA reduces each histogram to the pair's exact
+// moments (sum c ln c as 128-bit fixed point, non-empty cells) or, in counts
+// mode, writes the cumulative histograms out.
 __device__ __forceinline__ uint64_t tri_index(uint64_t i, uint64_t j, uint64_t n) {
   // row-major index of pair (i, j), i < j, among all pairs of n items
   return i * n - i * (i + 1) / 2 + (j - i - 1);
 }
 
-template <bool kCounts>
+constexpr int kTabHist = 1024;  // 128-bit c ln c entries kept in shared memory
+
+__device__ __forceinline__ void red_shared_inc(uint32_t addr) {
+  asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr) : "memory");
+}
+
+// c ln c beyond the shared table (rare): kept out of line.
+__device__ __noinline__ U128 clnc_far_u128(const double *__restrict__ gtab, unsigned c) {
+  return u128_from_double((c < (unsigned)kTabGlobal) ? __ldg(gtab + c) : clnc_value(c));
+}
+
+template <int R, int C, bool kCounts>
 __global__ void __launch_bounds__(512)
-pairs_atomic_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__ tasks,
-                    const __grid_constant__ PairParams P,
-                    const U128 *__restrict__ clnc_tab, U128 *__restrict__ sclnc,
-                    unsigned *__restrict__ nnz,
-                    unsigned *__restrict__ counts, int *__restrict__ flag) {
+pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__ tasks,
+                  const __grid_constant__ PairParams P, const double *__restrict__ gtab,
+                  U128 *__restrict__ sclnc, unsigned *__restrict__ nnz,
+                  unsigned *__restrict__ counts, int *__restrict__ flag) {
+  constexpr int NP = R * C;
   extern __shared__ __align__(16) unsigned char dyn[];
-  unsigned *hist = reinterpret_cast<unsigned *>(dyn);
-  __shared__ U128 tab[kTabSmem];
-  __shared__ uint32_t rows[16], cols[16];
-  __shared__ uint64_t outidx[16];
-  __shared__ int nr_s, nc_s, np_s, badflag;
-  const int tid = threadIdx.x;
   const int nb = P.nb, nb2 = nb * nb;
+  unsigned *hist = reinterpret_cast<unsigned *>(dyn);
+  U128 *tab = reinterpret_cast<U128 *>(dyn + (((size_t)NP * nb2 * 4 + 15) & ~size_t(15)));
+  __shared__ uint32_t rows_s[R], cols_s[C];
+  __shared__ uint64_t out_s[NP];
+  const int tid = threadIdx.x;
   const uint64_t n = P.nframes;
 
   if (tid == 0) {
-    badflag = 0;
     if (P.all_pairs) {
-      // implicit upper-triangular task grid over R x R tiles
+      // implicit upper-triangular grid of R x R tiles (R == C)
       const uint64_t T = P.ntile;
       uint64_t id = blockIdx.x, bi = 0;
-      // invert id = bi*T - bi*(bi-1)/2 + (bj - bi)
       while (true) {
-        uint64_t rowlen = T - bi;
+        const uint64_t rowlen = T - bi;
         if (id < rowlen) break;
         id -= rowlen;
         ++bi;
       }
       const uint64_t bj = bi + id;
-      int nr = 0, nc = 0, np = 0;
-      for (int r = 0; r < P.tile; ++r)
-        if (bi * P.tile + r < P.ndof) rows[nr++] = (uint32_t)(bi * P.tile + r);
-      for (int c = 0; c < P.tile; ++c)
-        if (bj * P.tile + c < P.ndof) cols[nc++] = (uint32_t)(bj * P.tile + c);
-      for (int r = 0; r < nr; ++r)
-        for (int c = 0; c < nc; ++c) {
-          uint32_t i = rows[r], j = cols[c];
-          outidx[r * nc + c] = (i < j) ? tri_index(i, j, P.ndof) : ~0ull;
-          ++np;
+      for (int r = 0; r < R; ++r) {
+        const uint64_t i = bi * R + r;
+        rows_s[r] = (uint32_t)(i < P.ndof ? i : bi * R);
+      }
+      for (int c = 0; c < C; ++c) {
+        const uint64_t j = bj * C + c;
+        cols_s[c] = (uint32_t)(j < P.ndof ? j : bj * C);
+      }
+      for (int r = 0; r < R; ++r)
+        for (int c = 0; c < C; ++c) {
+          const uint64_t i = bi * R + r, j = bj * C + c;
+          out_s[r * C + c] = (i < j && j < P.ndof) ? tri_index(i, j, P.ndof) : ~0ull;
         }
-      nr_s = nr;
-      nc_s = nc;
-      np_s = nr * nc;
     } else {
       const PairTask &tk = tasks[blockIdx.x];
-      for (int r = 0; r < tk.nr; ++r) rows[r] = tk.rows[r];
-      for (int c = 0; c < tk.nc; ++c) cols[c] = tk.cols[c];
-      for (int q = 0; q < tk.nr * tk.nc; ++q) outidx[q] = tk.out[q];
-      nr_s = tk.nr;
-      nc_s = tk.nc;
-      np_s = tk.nr * tk.nc;
+      for (int r = 0; r < R; ++r) rows_s[r] = tk.rows[r < tk.nr ? r : 0];
+      for (int c = 0; c < C; ++c) cols_s[c] = tk.cols[c < tk.nc ? c : 0];
+      for (int r = 0; r < R; ++r)
+        for (int c = 0; c < C; ++c)
+          out_s[r * C + c] = (r < tk.nr && c < tk.nc) ? tk.out[r * tk.nc + c] : ~0ull;
     }
   }
-  for (int i = tid; i < kTabSmem; i += blockDim.x) tab[i] = clnc_tab[i];
-  __syncthreads();
-  const int nr = nr_s, nc = nc_s, np = np_s;
-  for (int i = tid; i < np * nb2; i += blockDim.x) hist[i] = 0;
+  for (int i = tid; i < kTabHist; i += blockDim.x) tab[i] = u128_from_double(__ldg(gtab + i));
+  for (int i = tid; i < NP * nb2; i += blockDim.x) hist[i] = 0;
   __syncthreads();
 
-  const uint8_t *rp[4], *cp[16];
-  for (int r = 0; r < nr; ++r) rp[r] = bins + ((uint64_t)rows[r] * P.nschemes + P.scheme) * n;
-  for (int c = 0; c < nc; ++c) cp[c] = bins + ((uint64_t)cols[c] * P.nschemes + P.scheme) * n;
+  const uint32_t hist_s = (uint32_t)__cvta_generic_to_shared(hist);
+  // DOF rows as 32-bit word offsets (row starts are 4-byte aligned when the
+  // word path is used; the byte path rebuilds the byte offset)
+  const uint32_t *bw = reinterpret_cast<const uint32_t *>(bins);
+  uint32_t rw0[R], cw0[C];
+  uint32_t rconst[R], cconst[C];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    rw0[r] = (uint32_t)((((uint64_t)rows_s[r] * P.nschemes + P.scheme) * n) >> 2);
+    rconst[r] = hist_s + 4u * (uint32_t)(r * C * nb2);
+  }
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    cw0[c] = (uint32_t)((((uint64_t)cols_s[c] * P.nschemes + P.scheme) * n) >> 2);
+    cconst[c] = 4u * (uint32_t)(c * nb2);
+  }
+  const uint32_t nb4 = 4u * (uint32_t)nb;
+  const uint32_t lim = 0x01010101u * (uint32_t)nb;
   const bool word = (n & 3) == 0;
   int bad = 0;
+
+  auto one_frame = [&](uint64_t f) {
+    uint32_t a[R], b[C];
+    bool ok = true;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      a[r] = bins[((uint64_t)rows_s[r] * P.nschemes + P.scheme) * n + f];
+      ok &= a[r] < (uint32_t)nb;
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      b[c] = bins[((uint64_t)cols_s[c] * P.nschemes + P.scheme) * n + f];
+      ok &= b[c] < (uint32_t)nb;
+    }
+    if (!ok) {
+      bad = 1;
+      return;
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+      for (int c = 0; c < C; ++c) red_shared_inc(rconst[r] + a[r] * nb4 + cconst[c] + 4u * b[c]);
+  };
 
   for (int t = 0; t < P.nsteps; ++t) {
     const uint64_t f0 = (uint64_t)t * P.step_size, f1 = f0 + P.step_size;
     if (word) {
-      const uint64_t g0 = f0 >> 2, g1 = (f1 + 3) >> 2;
+      const uint64_t g0 = (f0 + 3) >> 2, g1 = f1 >> 2;   // whole 4-frame groups
+      for (uint64_t f = f0 + tid; f < min(f1, g0 << 2); f += blockDim.x) one_frame(f);
+      for (uint64_t f = max(f0, g1 << 2) + tid; f < f1; f += blockDim.x) one_frame(f);
       for (uint64_t g = g0 + tid; g < g1; g += blockDim.x) {
-        const uint64_t fb = g << 2;
-        unsigned rv[4], cv[16];
-        for (int r = 0; r < nr; ++r) rv[r] = __ldg(reinterpret_cast<const unsigned *>(rp[r]) + g);
-        for (int c = 0; c < nc; ++c) cv[c] = __ldg(reinterpret_cast<const unsigned *>(cp[c]) + g);
+        uint32_t rw[R], cw[C];
+        uint32_t v = 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          rw[r] = __ldg(bw + rw0[r] + (uint32_t)g);
+          v |= __vcmpgeu4(rw[r], lim);
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+          cw[c] = __ldg(bw + cw0[c] + (uint32_t)g);
+          v |= __vcmpgeu4(cw[c], lim);
+        }
+        if (v) {
+          bad = 1;
+          continue;
+        }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          const uint64_t f = fb + q;
-          if (f < f0 || f >= f1) continue;
-          for (int r = 0; r < nr; ++r) {
-            const unsigned a = (rv[r] >> (8 * q)) & 255u;
-            for (int c = 0; c < nc; ++c) {
-              const unsigned b = (cv[c] >> (8 * q)) & 255u;
-              if (a < (unsigned)nb && b < (unsigned)nb)
-                atomicAdd(&hist[(r * nc + c) * nb2 + a * nb + b], 1u);
-              else
-                bad = 1;
-            }
-          }
+          uint32_t ro[R], co[C];
+#pragma unroll
+          for (int r = 0; r < R; ++r) ro[r] = rconst[r] + ((rw[r] >> (8 * q)) & 255u) * nb4;
+#pragma unroll
+          for (int c = 0; c < C; ++c) co[c] = cconst[c] + ((cw[c] >> (8 * q)) & 255u) * 4u;
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int c = 0; c < C; ++c) red_shared_inc(ro[r] + co[c]);
         }
       }
     } else {
-      for (uint64_t f = f0 + tid; f < f1; f += blockDim.x) {
-        for (int r = 0; r < nr; ++r) {
-          const unsigned a = rp[r][f];
-          for (int c = 0; c < nc; ++c) {
-            const unsigned b = cp[c][f];
-            if (a < (unsigned)nb && b < (unsigned)nb)
-              atomicAdd(&hist[(r * nc + c) * nb2 + a * nb + b], 1u);
-            else
-              bad = 1;
-          }
-        }
-      }
+      for (uint64_t f = f0 + tid; f < f1; f += blockDim.x) one_frame(f);
     }
     __syncthreads();
     if (kCounts) {
-      for (int q = 0; q < np; ++q) {
-        const uint64_t o = outidx[q];
+      for (int q = 0; q < NP; ++q) {
+        const uint64_t o = out_s[q];
         if (o == ~0ull) continue;
         unsigned *dst = counts + (o * P.nsteps + t) * (uint64_t)nb2;
         for (int i = tid; i < nb2; i += blockDim.x) dst[i] = hist[q * nb2 + i];
       }
     } else {
-      // one warp per pair: sum_c round(c ln c 2^32) and non-empty cells
+      // one warp per pair: exact sum of c ln c and non-empty cells
       const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
-      for (int q = warp; q < np; q += nwarps) {
-        const uint64_t o = outidx[q];
+      for (int q = warp; q < NP; q += nwarps) {
+        const uint64_t o = out_s[q];
         if (o == ~0ull) continue;
         U128 acc;
         acc.lo = acc.hi = 0ull;
-        unsigned cntnz = 0;
+        unsigned cz = 0;
         const unsigned *h = hist + q * nb2;
         for (int i = lane; i < nb2; i += 32) {
           const unsigned c = h[i];
-          acc = u128_add(acc, (c < (unsigned)kTabSmem) ? tab[c] : clnc_fixed(c));
-          cntnz += (c != 0);
+          const U128 v = (c < (unsigned)kTabHist) ? tab[c] : clnc_far_u128(gtab, c);
+          acc = u128_add(acc, v);
+          cz += (c != 0);
         }
         for (int off = 16; off; off >>= 1) {
           acc = u128_add(acc, u128_shfl_xor(acc, off));
-          cntnz += __shfl_xor_sync(0xffffffffu, cntnz, off);
+          cz += __shfl_xor_sync(0xffffffffu, cz, off);
         }
         if (lane == 0) {
           sclnc[o * P.nsteps + t] = acc;
-          nnz[o * P.nsteps + t] = cntnz;
+          nnz[o * P.nsteps + t] = cz;
         }
       }
     }
@@ -483,7 +529,7 @@ entropy2d_counts_kernel(const uint32_t *__restrict__ pairs, const uint8_t *__res
 }
 
 // ----------------------------------------------------------------------------
-int init_clnc_table(centre_ctx *ctx, U128 *tab) {
+int init_clnc_table(centre_ctx *ctx, double *tab) {
   clnc_table_kernel<<<(kTabGlobal + 255) / 256, 256, 0, ctx->stream>>>(tab, kTabGlobal);
   ctx->launches++;
   CENTRE_CUDA(ctx, cudaGetLastError());
@@ -502,33 +548,58 @@ int launch_entropy1d(centre_ctx *ctx, const EntParams &P, uint32_t ndof, const u
   return CENTRE_OK;
 }
 
+// Shared-memory budget of the histograms (the 128-bit c ln c table and the
+// kernel's static data take the rest of the 227 KB).
+static constexpr size_t kHistBudget = 184 * 1024;
+
 int pair_tile_for(int nb) {
   // pairs whose nb*nb uint32 histograms fit the shared-memory budget
-  const size_t budget = 192 * 1024;
   const size_t per = (size_t)nb * nb * 4;
-  int p = (int)std::min<size_t>(16, budget / per);
-  return p;
+  return (int)std::min<size_t>(16, kHistBudget / per);
+}
+
+template <int R, int C>
+static int launch_hist(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
+                       uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
+                       unsigned *d_counts) {
+  const size_t smem = (((size_t)R * C * P.nb * P.nb * 4 + 15) & ~size_t(15)) + 16 * kTabHist;
+  if (d_counts) {
+    CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pairs_hist_kernel<R, C, true><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
+        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+  } else {
+    CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pairs_hist_kernel<R, C, false><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
+        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+  }
+  return CENTRE_OK;
 }
 
 int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
-                        uint64_t ntasks, const U128 *d_tab, U128 *d_sclnc, unsigned *d_nnz,
+                        uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
                         unsigned *d_counts) {
   if (ntasks == 0) return CENTRE_OK;
-  const int ppair = P.all_pairs ? P.tile * P.tile : std::max(1, std::min(16, pair_tile_for(P.nb)));
   KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
-  size_t smem = (size_t)ppair * P.nb * P.nb * 4;
-  if (d_counts) {
-    CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_atomic_kernel<true>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    pairs_atomic_kernel<true><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
-        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+  int rc;
+  if (P.all_pairs) {
+    switch (P.tile) {
+      case 4: rc = launch_hist<4, 4>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts); break;
+      case 3: rc = launch_hist<3, 3>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts); break;
+      case 2: rc = launch_hist<2, 2>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts); break;
+      default: rc = launch_hist<1, 1>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts); break;
+    }
   } else {
-    CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_atomic_kernel<false>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    pairs_atomic_kernel<false><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
-        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+    const int w = pair_tile_for(P.nb);
+    if (w >= 16) rc = launch_hist<1, 16>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts);
+    else if (w >= 8) rc = launch_hist<1, 8>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts);
+    else if (w >= 4) rc = launch_hist<1, 4>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts);
+    else if (w >= 2) rc = launch_hist<1, 2>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts);
+    else rc = launch_hist<1, 1>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts);
   }
   ctx->launches++;
+  if (rc != CENTRE_OK) return rc;
   CENTRE_CUDA(ctx, cudaGetLastError());
   return CENTRE_OK;
 }

@@ -67,22 +67,28 @@ __device__ __forceinline__ U128 u128_shfl_xor(U128 v, int o) {
   return v;
 }
 
-// The double c*log(c) represented exactly as an integer multiple of 2^-60:
-// its 53-bit significand shifted by its exponent (c >= 2 gives an exponent
-// >= 0, so the shift is a left shift of at least 8 and nothing is rounded).
-// Integer sums of these are the exact sums of the per-cell doubles, so the
-// cell sum is independent of how cells are spread over threads, tiles or
-// count kernels.
-__device__ __forceinline__ U128 clnc_fixed(unsigned c) {
+// c*log(c) in double precision, the per-cell term of the joint entropy.
+// Every count form evaluates it through this one expression (or reads it
+// from the table the same expression filled), so all forms see identical
+// doubles.
+__device__ __forceinline__ double clnc_value(unsigned c) {
+  return (c < 2) ? 0.0 : (double)c * log((double)c);
+}
+
+// A non-negative double v (0 or >= 1) represented exactly as an integer
+// multiple of 2^-60: its 53-bit significand shifted by its exponent (v >= 1
+// gives a shift >= 60 - 52 = 8, so it is a left shift and nothing is
+// rounded).  Integer sums of these are the exact sums of the per-cell
+// doubles, so the cell sum is independent of how cells are spread over
+// threads, tiles or count kernels.
+__device__ __forceinline__ U128 u128_from_double(double v) {
   U128 r;
   r.lo = 0ull;
   r.hi = 0ull;
-  if (c < 2) return r;
-  const double v = (double)c * log((double)c);
+  if (v == 0.0) return r;
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-  const int e = (int)((bits >> 52) & 0x7ff) - 1023;
+  const int s = (int)((bits >> 52) & 0x7ff) - 1023 + 8;  // value = m * 2^(e - 52 + 60)
   const unsigned long long m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  const int s = e + 8;  // value = m * 2^(e - 52 + 60)
   if (s >= 64) {
     r.hi = m << (s - 64);
   } else {
@@ -92,17 +98,19 @@ __device__ __forceinline__ U128 clnc_fixed(unsigned c) {
   return r;
 }
 
+__device__ __forceinline__ U128 clnc_fixed(unsigned c) { return u128_from_double(clnc_value(c)); }
+
 __host__ __device__ __forceinline__ double u128_value(U128 x) {
   return (double)x.hi * 16.0 + (double)x.lo * 0x1p-60;
 }
 
-int init_clnc_table(centre_ctx *ctx, U128 *tab);
+int init_clnc_table(centre_ctx *ctx, double *tab);
 int launch_entropy1d(centre_ctx *ctx, const EntParams &P, uint32_t ndof, const uint8_t *d_types,
                      const uint8_t *d_bins, const double *d_ext, double *d_s1,
                      unsigned long long *d_freq, double *d_lsum);
 int pair_tile_for(int nb);
 int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
-                        uint64_t ntasks, const U128 *d_tab, U128 *d_sclnc, unsigned *d_nnz,
+                        uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
                         unsigned *d_counts);
 int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uint32_t *d_pairs,
                       int all_pairs, uint32_t ndof, const double *d_ext, const double *d_lsum,
@@ -120,7 +128,7 @@ int launch_discretize(centre_ctx *ctx, int bat_type, const float *d_data, uint32
 
 // pairs_tc.cu
 bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes);
-int launch_pairs_tc(centre_ctx *ctx, const PairParams &P, const U128 *d_tab, U128 *d_sclnc,
+int launch_pairs_tc(centre_ctx *ctx, const PairParams &P, const double *d_tab, U128 *d_sclnc,
                     unsigned *d_nnz);
 
 // score.cu

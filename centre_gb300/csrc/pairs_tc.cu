@@ -17,7 +17,9 @@
 // byte per (frame, DOF) into the K-major, 128-byte-swizzled tiles and clear
 // exactly those bytes again once the MMA has consumed the stage, so building
 // a one-hot tile costs two byte stores per (frame, DOF) instead of writing
-// the whole tile.
+// the whole tile.  Lane l of a producer warp owns frames 4l..4l+3 of the
+// chunk for every DOF of the tile: its bins arrive in one coalesced 32-bit
+// load per DOF, and the stores of one instruction spread over all 32 banks.
 //
 // Convergence steps are prefixes of the frame axis: K-chunks never straddle a
 // step boundary, and at each boundary the epilogue warps read the running
@@ -26,8 +28,11 @@
 // add them into the pair's moments with integer atomics (tiles split pair
 // blocks; integer addition keeps the result independent of the split).
 //
-// Warp roles (256 threads): warp 0 allocates TMEM and one lane issues the
-// MMAs; warps 1-3 produce operand stages; warps 4-7 run the epilogue.  Every
+// Warp roles (288 threads): warp 0 allocates TMEM and one lane issues the
+// MMAs; warps 1-4 produce operand stages, warp 1+p owning stage p, so four
+// stages are built concurrently without cross-warp barriers, each warp
+// prefetching the bins of its next chunk into registers while it marks the
+// current one; warps 5-8 run the epilogue (TMEM lane group = warp % 4).  Every
 // mbarrier wait is bounded: on expiry the kernel sets an error flag, lets the
 // MMAs it issued drain (again bounded), frees its TMEM and returns.
 #include <algorithm>
@@ -50,10 +55,11 @@ constexpr int kMinBins = 16;                // DOF slots per tile bounded below
 constexpr int kMaxSlotsA = kTileM / kMinBins + 1;  // 9
 constexpr int kMaxSlotsB = kTileN / kMinBins + 1;  // 17
 constexpr int kMaxSlots = kMaxSlotsA + kMaxSlotsB;
-constexpr int kTabTc = 512;                 // c ln c entries in shared memory
-constexpr int kProducers = 96;
+constexpr int kTabTc = 2048;                // c ln c doubles in shared memory
+constexpr int kProducerWarps = kStages;     // producer warp p owns stage p
 constexpr int kEpilogue = 128;
-constexpr int kThreads = 256;
+constexpr int kThreads = 32 * (1 + kProducerWarps + 4);   // 288
+constexpr int kFramesPerLane = kChunk / 32;              // 4
 constexpr unsigned kTmemCols = 256;
 constexpr long long kWaitCycles = 20000000000ll;  // ~10 s at 2 GHz
 constexpr uint8_t kOne = 0x38;              // 1.0 in E4M3
@@ -88,12 +94,8 @@ struct Smem {
   uint64_t drain;
   uint32_t tmem_base;
   int abort_flag;
-  int pgo[2];       // producers' per-iteration go/abort decision
   int ego[2];       // epilogue's per-snapshot go/abort decision
-  StageMeta meta[kStages];
-  uint16_t col_dof[kTileN];
-  uint8_t sbins[kStages][kMaxSlots][kChunk];
-  U128 tab[kTabTc];
+  double tab[kTabTc];
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -215,65 +217,123 @@ __device__ __forceinline__ void tile_geometry(const TcParams &P, uint2 tl, Stage
   m.ndb = lastb / P.nb - m.d0b + 1;
 }
 
-// Set (val = kOne) or clear (val = 0) the one-hot bytes of one stage.
-__device__ void stage_marks(const TcParams &P, Smem &S, uint8_t *stage, int s, const StageMeta &m,
-                            uint8_t val, int ptid) {
-  uint8_t *A = stage;
-  uint8_t *B = stage + kABytes;
-  const int nslots = m.nda + m.ndb;
-  const int units = nslots * (kChunk / 16);
-  for (int u = ptid; u < units; u += kProducers) {
-    const int slot = u >> 3, g = u & 7;
-    const bool isA = slot < m.nda;
-    const int dof = isA ? m.d0a + slot : m.d0b + (slot - m.nda);
-    const int base = dof * P.nb - (isA ? m.rb : m.cb);
-    const int rows = isA ? kTileM : kTileN;
-    uint8_t *T = isA ? A : B;
-    const uint8_t *sb = S.sbins[s][slot] + g * 16;
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int k = g * 16 + q;
-      if (k >= m.nvalid) break;
-      const int row = base + (int)sb[q];
-      if (row >= 0 && row < rows) T[swz((uint32_t)row, (uint32_t)k)] = val;
+// Chunk c of a CTA's work: tile and frame range.  Walks the per-tile chunk
+// sequence (steps x 128-frame chunks, a chunk never straddles a step).
+struct ChunkPos {
+  uint64_t ti;      // tile index (global)
+  uint64_t f0, f1;
+  bool last;        // closes a convergence step
+  bool valid;
+};
+
+struct ChunkWalker {
+  uint64_t ti;
+  ChunkIter it;
+  uint64_t stride;
+  uint64_t ntiles;
+  __device__ void start(uint64_t first, uint64_t stride_, uint64_t ntiles_, uint64_t ss, int ns) {
+    ti = first;
+    stride = stride_;
+    ntiles = ntiles_;
+    it.start(ss, ns);
+  }
+  __device__ ChunkPos next() {
+    ChunkPos p;
+    p.valid = false;
+    while (ti < ntiles) {
+      if (it.next(p.f0, p.f1, p.last)) {
+        p.ti = ti;
+        p.valid = true;
+        return p;
+      }
+      ti += stride;
+      it.start(it.ss, it.nsteps);
     }
+    return p;
+  }
+};
+
+// Slot geometry of a stage: DOF slot -> (A or B tile, first row of the DOF's
+// bins relative to the tile).
+__device__ __forceinline__ void slot_info(const TcParams &P, const StageMeta &m, int slot,
+                                          bool &isA, int &dof, int &base) {
+  isA = slot < m.nda;
+  dof = isA ? m.d0a + slot : m.d0b + (slot - m.nda);
+  base = dof * P.nb - (isA ? m.rb : m.cb);
+}
+
+// Load lane's 4 frames (4*lane .. +3 of the chunk) of every DOF slot into
+// registers.  The values are first used one chunk later (prefetch); the
+// range check happens when they are marked.
+__device__ __forceinline__ void load_lane_bins(const TcParams &P, const StageMeta &m, uint64_t f0,
+                                               int lane, uint32_t (&pb)[kMaxSlots], int *flag) {
+  const int nslots = m.nda + m.ndb;
+  const uint64_t n = P.nframes;
+  const int k0 = kFramesPerLane * lane;
+  const int avail = max(0, min(kFramesPerLane, m.nvalid - k0));
+#pragma unroll
+  for (int slot = 0; slot < kMaxSlots; ++slot) {
+    uint32_t w = 0;
+    if (slot < nslots && avail > 0) {
+      bool isA;
+      int dof, base;
+      slot_info(P, m, slot, isA, dof, base);
+      if (dof < (int)P.ndof) {
+        const uint8_t *src = P.bins + ((uint64_t)dof * P.nschemes + P.scheme) * n + f0 + k0;
+        if (avail == kFramesPerLane && ((reinterpret_cast<uintptr_t>(src) & 3u) == 0)) {
+          w = __ldg(reinterpret_cast<const uint32_t *>(src));
+        } else {
+#pragma unroll
+          for (int q = 0; q < kFramesPerLane; ++q)
+            if (q < avail) w |= (uint32_t)__ldg(src + q) << (8 * q);
+        }
+      }
+    }
+    pb[slot] = w;
   }
 }
 
-// Load the bins of a stage's DOFs for frames [f0, f0 + nvalid) into smem.
-__device__ void stage_load_bins(const TcParams &P, Smem &S, int s, const StageMeta &m, uint64_t f0,
-                                int ptid, int *flag) {
+// c ln c for counts beyond the shared-memory table (rare): the global table,
+// then the expression itself.  Kept out of line so the unrolled epilogue
+// loop stays small.
+__device__ __noinline__ double clnc_far(const double *__restrict__ gtab, unsigned c) {
+  return (c < (unsigned)kTabGlobal) ? __ldg(gtab + c) : clnc_value(c);
+}
+
+__device__ __forceinline__ void sts_u8(uint32_t addr, uint32_t v) {
+  asm volatile("st.shared.u8 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+
+// Write val at the one-hot positions of the lane's frames.  In a K-major
+// 128B-swizzled tile, element (row, k) sits at
+//   (row << 7) + ((((k >> 4) ^ row) & 7) << 4) + (k & 15).
+__device__ __forceinline__ void mark_lane(const TcParams &P, const StageMeta &m, uint32_t stage_s,
+                                          int lane, uint32_t (&pb)[kMaxSlots], uint32_t val,
+                                          bool check, int *flag) {
   const int nslots = m.nda + m.ndb;
-  const int units = nslots * (kChunk / 16);
-  const uint64_t n = P.nframes;
-  for (int u = ptid; u < units; u += kProducers) {
-    const int slot = u >> 3, g = u & 7;
-    const int dof = slot < m.nda ? m.d0a + slot : m.d0b + (slot - m.nda);
-    uint8_t *dst = S.sbins[s][slot] + g * 16;
-    if (dof >= (int)P.ndof) {
-      *reinterpret_cast<uint4 *>(dst) = make_uint4(0, 0, 0, 0);
-      continue;
-    }
-    const uint8_t *src = P.bins + ((uint64_t)dof * P.nschemes + P.scheme) * n + f0 + g * 16;
-    const int avail = max(0, min(16, m.nvalid - g * 16));
-    uint4 v = make_uint4(0, 0, 0, 0);
-    if (avail == 16 && ((reinterpret_cast<uintptr_t>(src) & 15u) == 0)) {
-      v = __ldg(reinterpret_cast<const uint4 *>(src));
-    } else {
-      uint8_t tmp[16];
+  const int k0 = kFramesPerLane * lane;
+  const uint32_t g = (uint32_t)(k0 >> 4);
+  const uint32_t q0 = (uint32_t)(k0 & 15);
+  const int kv = m.nvalid - k0;
 #pragma unroll
-      for (int q = 0; q < 16; ++q) tmp[q] = (q < avail) ? __ldg(src + q) : (uint8_t)0;
-      v = *reinterpret_cast<uint4 *>(tmp);
-    }
-    // bins must lie below nb: check four bytes at a time
-    const uint32_t lim = 0x01010101u * (uint32_t)P.nb;
-    uint32_t bad = __vcmpgeu4(v.x, lim) | __vcmpgeu4(v.y, lim) | __vcmpgeu4(v.z, lim) |
-                   __vcmpgeu4(v.w, lim);
-    if (bad) {
+  for (int slot = 0; slot < kMaxSlots; ++slot) {
+    if (slot >= nslots) break;
+    bool isA;
+    int dof, base;
+    slot_info(P, m, slot, isA, dof, base);
+    const uint32_t rows = isA ? kTileM : kTileN;
+    const uint32_t T = stage_s + (isA ? 0u : (uint32_t)kABytes);
+    if (check && __vcmpgeu4(pb[slot], 0x01010101u * (uint32_t)P.nb)) {
+      // a bin >= nb: report it and keep every store inside the tile
       atomicOr(flag, kFlagBinRange);
-      v = make_uint4(0, 0, 0, 0);  // keep the kernel in bounds; the call reports the error
+      pb[slot] = 0;
     }
-    *reinterpret_cast<uint4 *>(dst) = v;
+#pragma unroll
+    for (int q = 0; q < kFramesPerLane; ++q) {
+      if (q >= kv) break;
+      const uint32_t row = (uint32_t)(base + (int)((pb[slot] >> (8 * q)) & 255u));
+      if (row < rows) sts_u8(T + (row << 7) + (((g ^ row) & 7u) << 4) + q0 + q, val);
+    }
   }
 }
 
@@ -281,7 +341,7 @@ __device__ void stage_load_bins(const TcParams &P, Smem &S, int s, const StageMe
 // lanes of a warp hold consecutive rows, so rows of the same DOF are
 // contiguous lanes; a segmented shuffle reduction leaves each DOF's total in
 // its first lane, which adds it to the pair's moments.
-__device__ __forceinline__ void flush_segment(const TcParams &P, U128 a, unsigned z, int rd,
+__device__ __noinline__ void flush_segment(const TcParams &P, U128 a, unsigned z, int rd,
                                               bool rowvalid, int cd, int t, int lane,
                                               U128 *__restrict__ sclnc,
                                               unsigned *__restrict__ nnz) {
@@ -311,12 +371,13 @@ __device__ __forceinline__ void flush_segment(const TcParams &P, U128 a, unsigne
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-pairs_tc_kernel(const __grid_constant__ TcParams P, const U128 *__restrict__ gtab,
+pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ gtab,
                 U128 *__restrict__ sclnc, unsigned *__restrict__ nnz, int *__restrict__ flag) {
   extern __shared__ __align__(1024) unsigned char dyn[];
   // stages first (1024-aligned), then the bookkeeping block
-  uintptr_t basep = (reinterpret_cast<uintptr_t>(dyn) + 1023) & ~uintptr_t(1023);
-  uint8_t *stages = reinterpret_cast<uint8_t *>(basep);
+  const uint32_t pad = (1024u - (smem_u32(dyn) & 1023u)) & 1023u;
+  uint8_t *stages = dyn + pad;
+  const uint32_t stages_s = smem_u32(stages);
   Smem &S = *reinterpret_cast<Smem *>(stages + kStages * kStageBytes);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -329,9 +390,8 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const U128 *__restrict__ gta
   }
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&S.full[s], kProducers);
+      mbar_init(&S.full[s], 32);
       mbar_init(&S.empty[s], 1);
-      S.meta[s].used = 0;
     }
     mbar_init(&S.accfull, 1);
     mbar_init(&S.accempty, kEpilogue);
@@ -403,61 +463,61 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const U128 *__restrict__ gta
       }
     }
     __syncwarp();
-  } else if (warp <= 3) {
-    // ---- producers -----------------------------------------------------------
-    const int ptid = tid - 32;
-    uint32_t piter = 0;
-    int s = 0;
-    uint32_t ph[kStages] = {0, 0, 0, 0};
-    bool ok = true;
-    for (uint64_t ti = blockIdx.x; ti < P.ntiles && ok; ti += gridDim.x) {
-      StageMeta m;
-      tile_geometry(P, P.tiles[ti], m);
-      ChunkIter it;
-      it.start(P.step_size, P.nsteps);
-      uint64_t f0, f1;
-      bool last;
-      while (it.next(f0, f1, last)) {
-        // one thread waits for the stage and decides for the group
-        if (ptid == 0) {
-          bool go = true;
-          if (S.meta[s].used) {
-            go = wait_bar(S, &S.empty[s], ph[s], flag);
-            ph[s] ^= 1u;
-          }
-          if (*(volatile int *)&S.abort_flag) go = false;
-          S.pgo[piter & 1] = go ? 1 : 0;
-        }
-        named_bar(1, kProducers);
-        if (!*(volatile int *)&S.pgo[piter & 1]) { ok = false; break; }
-        ++piter;
-        uint8_t *stage = stages + s * kStageBytes;
-        if (S.meta[s].used) stage_marks(P, S, stage, s, S.meta[s], 0, ptid);
-        named_bar(1, kProducers);
-        m.nvalid = (int)(f1 - f0);
-        m.used = 1;
-        stage_load_bins(P, S, s, m, f0, ptid, flag);
-        named_bar(1, kProducers);
-        stage_marks(P, S, stage, s, m, kOne, ptid);
-        if (ptid == 0) S.meta[s] = m;
-        fence_proxy_async();
-        mbar_arrive(&S.full[s]);
-        s = (s + 1) % kStages;
+  } else if (warp <= kProducerWarps) {
+    // ---- producers: warp 1+p builds every chunk c with c % 4 == p ------------
+    const int p = warp - 1;
+    const uint32_t stage_s = stages_s + (uint32_t)(p * kStageBytes);
+    uint32_t ph = 0;
+    bool used = false;
+    StageMeta old;            // previous occupant of this stage
+    uint32_t oldb[kMaxSlots];
+    uint32_t pb[kMaxSlots];
+    ChunkWalker walk;
+    walk.start(blockIdx.x, gridDim.x, P.ntiles, P.step_size, P.nsteps);
+    ChunkPos cur;
+    for (int i = 0; i <= p; ++i) cur = walk.next();   // this warp's first chunk
+    StageMeta m;
+    if (cur.valid) {
+      tile_geometry(P, P.tiles[cur.ti], m);
+      m.nvalid = (int)(cur.f1 - cur.f0);
+      load_lane_bins(P, m, cur.f0, lane, pb, flag);
+    }
+    while (cur.valid) {
+      // wait until the MMA has consumed this stage's previous chunk
+      int go = 1;
+      if (lane == 0 && used) go = wait_bar(S, &S.empty[p], ph, flag) ? 1 : 0;
+      go = __shfl_sync(0xffffffffu, go, 0);
+      if (!go) break;
+      if (used) {
+        ph ^= 1u;
+        mark_lane(P, old, stage_s, lane, oldb, 0u, false, flag);
+      }
+      __syncwarp();
+      mark_lane(P, m, stage_s, lane, pb, kOne, true, flag);
+      fence_proxy_async();
+      mbar_arrive(&S.full[p]);
+      // remember what was set, then fetch this warp's next chunk
+      old = m;
+#pragma unroll
+      for (int i = 0; i < kMaxSlots; ++i) oldb[i] = pb[i];
+      used = true;
+      for (int i = 0; i < kProducerWarps; ++i) cur = walk.next();
+      if (cur.valid) {
+        tile_geometry(P, P.tiles[cur.ti], m);
+        m.nvalid = (int)(cur.f1 - cur.f0);
+        load_lane_bins(P, m, cur.f0, lane, pb, flag);
       }
     }
   } else {
     // ---- epilogue ------------------------------------------------------------
-    const int etid = tid - 128;          // 0..127 == accumulator row
-    const int ew = warp - 4;             // TMEM lane group
+    const int ew = warp & 3;             // TMEM lane group of this warp
+    const int etid = 32 * ew + lane;     // accumulator row
     uint32_t nsnap = 0;
     bool ok = true;
     const int nb = P.nb;
     for (uint64_t ti = blockIdx.x; ti < P.ntiles && ok; ti += gridDim.x) {
       StageMeta m;
       tile_geometry(P, P.tiles[ti], m);
-      named_bar(2, kEpilogue);   // previous tile's readers are done with col_dof
-      for (int c = etid; c < kTileN; c += kEpilogue) S.col_dof[c] = (uint16_t)((m.cb + c) / nb);
-      named_bar(2, kEpilogue);
       const int grow = m.rb + etid;
       const int rd = grow / nb;
       const bool rowvalid = grow < (int)P.nrows;
@@ -473,7 +533,8 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const U128 *__restrict__ gta
         U128 acc;
         acc.lo = acc.hi = 0ull;
         unsigned cnz = 0;
-        int cur = S.col_dof[0];
+        int cur = m.cb / nb;                       // column DOF of column 0
+        int nextb = (cur + 1) * nb - m.cb;         // first column of the next DOF
         for (int chunk = 0; chunk < kTileN / 32; ++chunk) {
           uint32_t v[32];
           const uint32_t taddr = tmem + ((uint32_t)(32 * ew) << 16) + (uint32_t)(chunk * 32);
@@ -492,21 +553,18 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const U128 *__restrict__ gta
 #pragma unroll
           for (int q = 0; q < 32; ++q) {
             const int c = chunk * 32 + q;
-            const int cd = S.col_dof[c];
-            if (cd != cur) {
+            if (c == nextb) {
               flush_segment(P, acc, cnz, rd, rowvalid, cur, t, lane, sclnc, nnz);
               acc.lo = acc.hi = 0ull;
               cnz = 0;
-              cur = cd;
+              ++cur;
+              nextb += nb;
             }
             // exact integer count from the FP32 accumulator
             const unsigned cnt = __float_as_uint(__uint_as_float(v[q]) + 8388608.0f) - 0x4B000000u;
             if (cnt) {
-              U128 add;
-              if (cnt < (unsigned)kTabTc) add = S.tab[cnt];
-              else if (cnt < (unsigned)kTabGlobal) add = gtab[cnt];
-              else add = clnc_fixed(cnt);
-              acc = u128_add(acc, add);
+              const double dv = (cnt < (unsigned)kTabTc) ? S.tab[cnt] : clnc_far(gtab, cnt);
+              acc = u128_add(acc, u128_from_double(dv));
               ++cnz;
             }
           }
@@ -541,7 +599,7 @@ bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes) {
   return true;
 }
 
-int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const U128 *d_tab, U128 *d_sclnc,
+int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const double *d_tab, U128 *d_sclnc,
                     unsigned *d_nnz) {
   const int nb = PP.nb;
   const uint32_t ndof = PP.ndof;

@@ -56,7 +56,7 @@ enum { CENTRE_NONE = 0, CENTRE_BOND = 1, CENTRE_ANGLE = 2, CENTRE_DIHEDRAL = 3 }
 enum { CENTRE_ML = 0, CENTRE_MM = 1, CENTRE_CS = 2, CENTRE_JS = 3 };
 /* How the 2-D joint counts are formed. */
 enum {
-  CENTRE_COUNTS_AUTO = 0,   /* one-hot tensor-core form where it applies  */
+  CENTRE_COUNTS_AUTO = 0,   /* histogram form where it fits, else TC      */
   CENTRE_COUNTS_ATOMIC = 1, /* shared-memory atomic histograms            */
   CENTRE_COUNTS_TC = 2      /* FP8 one-hot O^T O on tcgen05 tensor cores  */
 };
