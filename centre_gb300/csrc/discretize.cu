@@ -54,6 +54,7 @@ struct DiscParams {
   int nfit;              // coarse occupancy bins (torsions, optimize)
   double fit_bs;         // coarse bin size
   float xpi;             // smallest float x with RN(x + pi) >= 2pi
+  float xmax_ok;         // largest float accepted for this DOF type
   uint8_t schemes[kMaxSchemes];
   float tfit[kMaxFit + 1];   // tfit[k]: smallest x with coarse bin >= k
 };
@@ -84,11 +85,6 @@ __device__ __forceinline__ int ref_bin(float x, int dpind, double c, double lo,
   double v = shifted(x, dpind, c);
   double q = __ddiv_rn(__dsub_rn(v, lo), w);
   return (int)floor(q);
-}
-
-// Float bit patterns of non-negative floats are ordered like the floats.
-__device__ __forceinline__ float next_up(float x) {
-  return __int_as_float(__float_as_int(x) + 1);
 }
 
 // Smallest float x in [a, b] (non-negative, a <= b) with pred(x) true, given
@@ -215,10 +211,9 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
     two_sum(s_hi, x, s, e);
     s_hi = s;
     s_lo = __fadd_rn(s_lo, e);
-    // domain: bonds >= 0, angles in [0, pi], torsions in [0, 2pi)
-    if (!(x >= 0.f) || (P.type == 2 && (double)x > kPi) ||
-        (is_tor && (double)x >= kTwoPi))
-      bad = 1;
+    // domain: bonds >= 0, angles in [0, pi], torsions in [0, 2pi), finite;
+    // xmax_ok is the exact float image of the double bound
+    if (!(x >= 0.f && x <= P.xmax_ok)) bad = 1;
     if (is_tor) {
       if (x >= P.xpi) {
         cmin1 = fminf(cmin1, x);
@@ -658,6 +653,18 @@ int launch_discretize(centre_ctx *ctx, int bat_type, const float *d_data, uint32
   slice = (slice + 15) & ~uint64_t(15);
   P.slice = slice;
   P.staged = (slice * 4 <= kStageBytes) ? 1 : 0;
+  {
+    // largest float whose double value passes the reference's domain
+    float lim = FLT_MAX;
+    if (P.type == 2) {
+      lim = (float)kPi;
+      while ((double)lim > kPi) lim = nextafterf(lim, 0.0f);
+    } else if (P.type == 3) {
+      lim = (float)kTwoPi;
+      while ((double)lim >= kTwoPi) lim = nextafterf(lim, 0.0f);
+    }
+    P.xmax_ok = lim;
+  }
   if (P.type == 3) {
     P.nfit = (3 * (int)bins_ref > kMaxFit) ? kMaxFit : 3 * (int)bins_ref;
     P.fit_bs = ((kTwoPi + kDx) - 0.0) / P.nfit;   // src/Real2Int.cpp:281-284

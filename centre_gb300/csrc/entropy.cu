@@ -48,6 +48,7 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
   const uint64_t n = P.nframes, ss = P.step_size;
   const uint8_t *row = bins + ((uint64_t)dof * P.nschemes + s) * n;
   __shared__ unsigned hist[256];
+  __shared__ unsigned whist[8 * 256];   // per-warp histograms (256 threads)
   __shared__ unsigned long long cum[256];
   __shared__ double mids[256];
   __shared__ int badrange;
@@ -66,17 +67,46 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
   const int off = P.scheme_off[s];
   const uint64_t per = (uint64_t)P.nests * P.nschemes * P.nsteps;
 
+  const int warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const bool word = ((n & 3) == 0) && ((((uint64_t)dof * P.nschemes + s) * n & 3) == 0);
+  const uint32_t lim = 0x01010101u * (uint32_t)nb;
   for (int t = 0; t < P.nsteps; ++t) {
-    for (int b = tid; b < nb; b += blockDim.x) hist[b] = 0;
+    for (int b = tid; b < 8 * 256; b += blockDim.x) whist[b] = 0;
     __syncthreads();
     const uint64_t f0 = (uint64_t)t * ss, f1 = f0 + ss;
+    unsigned *wh = whist + warp * 256;
     int bad = 0;
-    for (uint64_t f = f0 + tid; f < f1; f += blockDim.x) {
-      unsigned v = row[f];
+    auto one = [&](uint64_t f) {
+      const unsigned v = row[f];
       if (v >= (unsigned)nb) bad = 1;
-      else atomicAdd(&hist[v], 1u);
+      else atomicAdd(&wh[v], 1u);
+    };
+    if (word) {
+      const uint64_t g0 = (f0 + 3) >> 2, g1 = f1 >> 2;
+      for (uint64_t f = f0 + tid; f < min(f1, g0 << 2); f += blockDim.x) one(f);
+      for (uint64_t f = max(f0, g1 << 2) + tid; f < f1; f += blockDim.x) one(f);
+      const uint32_t *rw = reinterpret_cast<const uint32_t *>(row);
+      for (uint64_t g = g0 + tid; g < g1; g += blockDim.x) {
+        const uint32_t w = __ldg(rw + g);
+        if (__vcmpgeu4(w, lim)) {
+          bad = 1;
+          continue;
+        }
+        atomicAdd(&wh[w & 255u], 1u);
+        atomicAdd(&wh[(w >> 8) & 255u], 1u);
+        atomicAdd(&wh[(w >> 16) & 255u], 1u);
+        atomicAdd(&wh[w >> 24], 1u);
+      }
+    } else {
+      for (uint64_t f = f0 + tid; f < f1; f += blockDim.x) one(f);
     }
     if (bad) badrange = 1;
+    __syncthreads();
+    for (int b = tid; b < nb; b += blockDim.x) {
+      unsigned h = 0;
+      for (int w = 0; w < nwarps; ++w) h += whist[w * 256 + b];
+      hist[b] = h;
+    }
     __syncthreads();
     for (int b = tid; b < nb; b += blockDim.x) cum[b] += hist[b];
     __syncthreads();
@@ -384,7 +414,7 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
 // S2 from the integer moments (ML, MM).  One thread per (pair, step) of a
 // scheme.
 __global__ void finalize2d_kernel(const uint32_t *__restrict__ pairs, int all_pairs,
-                                  uint32_t ndof, const double *__restrict__ ext,
+                                  uint32_t ndof, const double *__restrict__ logw,
                                   const double *__restrict__ lsum,
                                   const U128 *__restrict__ sclnc,
                                   const unsigned *__restrict__ nnz,
@@ -396,31 +426,41 @@ __global__ void finalize2d_kernel(const uint32_t *__restrict__ pairs, int all_pa
   const int t = (int)(idx % P.nsteps);
   uint32_t i, j;
   if (all_pairs) {
-    // invert the row-major upper-triangular index
-    const double nn = (double)ndof;
-    uint64_t r = (uint64_t)floor(((2 * nn - 1) - sqrt((2 * nn - 1) * (2 * nn - 1) - 8.0 * (double)p)) / 2);
-    while (r > 0 && r * ndof - r * (r + 1) / 2 > p) --r;
-    while ((r + 1) * ndof - (r + 1) * (r + 2) / 2 <= p) ++r;
-    i = (uint32_t)r;
-    j = (uint32_t)(p - (r * ndof - r * (r + 1) / 2) + r + 1);
+    tri_pair(p, ndof, i, j);
   } else {
     i = pairs[2 * p];
     j = pairs[2 * p + 1];
   }
-  const int nb = P.schemes[scheme];
-  double w1 = __ddiv_rn(__dsub_rn(ext[4 * i + 1], ext[4 * i]), (double)nb);
-  double w2 = __ddiv_rn(__dsub_rn(ext[4 * j + 1], ext[4 * j]), (double)nb);
-  if (P.kde) w1 = w2 = 1.0;
   const double nd = (t + 1.0) * (double)P.step_size;
   const double X = u128_value(sclnc[idx]);
   const double L = lsum[((uint64_t)i * P.nschemes + scheme) * P.nsteps + t] +
                    lsum[((uint64_t)j * P.nschemes + scheme) * P.nsteps + t];
-  const double S = log(nd) + log(w1 * w2) + (L - X) / nd;
+  // log(n A) = log n + log w_i + log w_j (per-step and per-DOF logs hoisted)
+  const double S = logw[(uint64_t)ndof * P.nschemes + t] +
+                   logw[(uint64_t)i * P.nschemes + scheme] + logw[(uint64_t)j * P.nschemes + scheme] +
+                   (L - X) / nd;
   const uint64_t per = (uint64_t)P.nests * P.nschemes * P.nsteps;
   for (int e = 0; e < P.nests; ++e) {
     double v = S;
     if (P.ests[e] == 1) v += ((double)nnz[idx] - 1.0) / (2.0 * nd);
     s2[p * per + ((uint64_t)e * P.nschemes + scheme) * P.nsteps + t] = v;
+  }
+}
+
+// log of each DOF's bin width per scheme (width 1 in KDE mode) followed by
+// log of the frame count of each step: the per-pair log(n A) is their sum.
+__global__ void logw_kernel(const double *__restrict__ ext, uint32_t ndof,
+                            const __grid_constant__ EntParams P, double *__restrict__ logw) {
+  const uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  const uint64_t nw = (uint64_t)ndof * P.nschemes;
+  if (idx < nw) {
+    const uint64_t d = idx / P.nschemes;
+    const int s = (int)(idx % P.nschemes);
+    const double w = __ddiv_rn(__dsub_rn(ext[4 * d + 1], ext[4 * d]), (double)P.schemes[s]);
+    logw[idx] = P.kde ? 0.0 : log(w);
+  } else if (idx < nw + (uint64_t)P.nsteps) {
+    const int t = (int)(idx - nw);
+    logw[idx] = log((t + 1.0) * (double)P.step_size);
   }
 }
 
@@ -610,9 +650,15 @@ int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uin
                       double *d_s2) {
   const uint64_t total = npairs * P.nsteps;
   if (total == 0) return CENTRE_OK;
+  int st = CENTRE_OK;
+  const uint64_t nl = (uint64_t)ndof * P.nschemes + P.nsteps;
+  double *d_logw = (double *)scratch(ctx, kSlotAux2, sizeof(double) * nl, &st);
+  if (!d_logw) return st;
+  // the table is rebuilt for each scheme (the same buffer serves all)
+  logw_kernel<<<(unsigned)((nl + 255) / 256), 256, 0, ctx->stream>>>(d_ext, ndof, P, d_logw);
   finalize2d_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(
-      d_pairs, all_pairs, ndof, d_ext, d_lsum, d_sclnc, d_nnz, P, scheme, npairs, d_s2);
-  ctx->launches++;
+      d_pairs, all_pairs, ndof, d_logw, d_lsum, d_sclnc, d_nnz, P, scheme, npairs, d_s2);
+  ctx->launches += 2;
   CENTRE_CUDA(ctx, cudaGetLastError());
   return CENTRE_OK;
 }

@@ -100,6 +100,22 @@ __device__ __forceinline__ U128 u128_from_double(double v) {
 
 __device__ __forceinline__ U128 clnc_fixed(unsigned c) { return u128_from_double(clnc_value(c)); }
 
+// Row-major upper-triangular pair (i, j), i < j, of index p among all pairs
+// of n items: a single-precision estimate of the row, corrected exactly with
+// integer arithmetic (no FP64 on the per-element path).
+__device__ __forceinline__ void tri_pair(uint64_t p, uint64_t n, uint32_t &i, uint32_t &j) {
+  const float nn = (float)n;
+  const float disc = (2.f * nn - 1.f) * (2.f * nn - 1.f) - 8.f * (float)p;
+  long long r = (long long)((2.f * nn - 1.f - sqrtf(fmaxf(disc, 0.f))) * 0.5f);
+  if (r < 0) r = 0;
+  if (r > (long long)n - 2) r = (long long)n - 2;
+  auto start = [n](long long rr) { return (uint64_t)rr * n - (uint64_t)rr * (uint64_t)(rr + 1) / 2; };
+  while (r > 0 && start(r) > p) --r;
+  while (r + 1 < (long long)n - 1 && start(r + 1) <= p) ++r;
+  i = (uint32_t)r;
+  j = (uint32_t)(p - start(r) + (uint64_t)r + 1);
+}
+
 __host__ __device__ __forceinline__ double u128_value(U128 x) {
   return (double)x.hi * 16.0 + (double)x.lo * 0x1p-60;
 }

@@ -52,13 +52,7 @@ __device__ __forceinline__ void pair_of(const ScoreParams &S, const uint32_t *pa
     j = pairs[2 * p + 1];
     return;
   }
-  const uint64_t n = S.ndof;
-  const double nn = (double)n;
-  uint64_t r = (uint64_t)floor(((2 * nn - 1) - sqrt((2 * nn - 1) * (2 * nn - 1) - 8.0 * (double)p)) / 2);
-  while (r > 0 && r * n - r * (r + 1) / 2 > p) --r;
-  while ((r + 1) * n - (r + 1) * (r + 2) / 2 <= p) ++r;
-  i = (uint32_t)r;
-  j = (uint32_t)(p - (r * n - r * (r + 1) / 2) + r + 1);
+  tri_pair(p, S.ndof, i, j);
 }
 
 // Rank of a pair in the reference's edge list: blocks B/B, B/A, B/D, A/A,
