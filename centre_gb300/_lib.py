@@ -83,6 +83,8 @@ _SIGS = {
                                        _vp, C.c_uint64, _vp, _vp]),
     "centre_gpu_entropy2d_dev": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp,
                                            _vp, _vp, C.c_uint64, _vp, _vp]),
+    "centre_gpu_entropy2d_static": (C.c_int, [C.POINTER(EntropyParams), C.c_uint32, _vp, _vp,
+                                              _vp, _vp, _vp]),
     "centre_gpu_counts2d": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp,
                                       C.c_uint64, _vp, _vp]),
     "centre_gpu_pair_moments": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp,

@@ -663,6 +663,23 @@ int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uin
   return CENTRE_OK;
 }
 
+// As launch_finalize2d, with the log table supplied by the caller instead of
+// context scratch (used by the entry point that allocates nothing).
+int launch_finalize2d_into(centre_ctx *ctx, const EntParams &P, int scheme, uint32_t ndof,
+                           const double *d_ext, const double *d_lsum, const U128 *d_sclnc,
+                           const unsigned *d_nnz, uint64_t npairs, double *d_logw,
+                           double *d_s2) {
+  const uint64_t total = npairs * P.nsteps;
+  if (total == 0) return CENTRE_OK;
+  const uint64_t nl = (uint64_t)ndof * P.nschemes + P.nsteps;
+  logw_kernel<<<(unsigned)((nl + 255) / 256), 256, 0, ctx->stream>>>(d_ext, ndof, P, d_logw);
+  finalize2d_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(
+      nullptr, 1, ndof, d_logw, d_lsum, d_sclnc, d_nnz, P, scheme, npairs, d_s2);
+  ctx->launches += 2;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  return CENTRE_OK;
+}
+
 int launch_entropy2d_counts(centre_ctx *ctx, const EntParams &P, int scheme,
                             const uint32_t *d_pairs, const uint8_t *d_types, const double *d_ext,
                             const unsigned *d_counts, uint64_t p0, uint64_t np, uint64_t npairs,

@@ -132,6 +132,10 @@ int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uin
                       int all_pairs, uint32_t ndof, const double *d_ext, const double *d_lsum,
                       const U128 *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
                       double *d_s2);
+int launch_finalize2d_into(centre_ctx *ctx, const EntParams &P, int scheme, uint32_t ndof,
+                           const double *d_ext, const double *d_lsum, const U128 *d_sclnc,
+                           const unsigned *d_nnz, uint64_t npairs, double *d_logw,
+                           double *d_s2);
 int launch_entropy2d_counts(centre_ctx *ctx, const EntParams &P, int scheme,
                             const uint32_t *d_pairs, const uint8_t *d_types, const double *d_ext,
                             const unsigned *d_counts, uint64_t p0, uint64_t np, uint64_t npairs,

@@ -157,6 +157,29 @@ int centre_gpu_entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p,
                              uint64_t npairs, const uint32_t *pairs,
                              double *s2);
 
+/* The all-pairs case of centre_gpu_entropy2d_dev without allocating any
+ * memory: no context is needed, all scratch space comes from one fixed
+ * device array of 16 MiB inside the library.  No counterpart in the
+ * reference, which allocates host memory per pair.  It serves callers that
+ * must not call cudaMalloc: code running while its stream is captured into a
+ * CUDA graph, plug-ins whose host application owns all device memory, and
+ * loops where an allocation could stall on a device synchronisation.
+ *   - Device pointers, enqueued on `cuda_stream`; returns after the stream
+ *     has finished the call (it reads back an error flag).
+ *   - ML and Miller-Madow estimators, shared-memory histogram counts only
+ *     (CENTRE_E_UNSUPPORTED otherwise).
+ *   - Sizes whose scratch exceeds the array (about 780,000 pair-steps, e.g.
+ *     400 DOFs with 10 steps) are rejected with CENTRE_E_ARG before anything
+ *     runs; larger problems use centre_gpu_entropy2d_dev.
+ *   - The first call on a device records the array's address and fills a
+ *     table in it; make that first call before any stream capture.
+ *   - Every call on a device shares the array: calls that overlap on the GPU
+ *     (other streams, other host threads) race and must be serialised. */
+int centre_gpu_entropy2d_static(const centre_entropy_params *p, uint32_t ndof,
+                                const uint8_t *types, const uint8_t *bins,
+                                const double *extremes, double *s2,
+                                void *cuda_stream);
+
 /* Joint counts only, for parity checks of the count kernels: binData2D
  * (src/Estimators.cpp:130-205) per pair.  freq [npairs][nsteps][sum nb^2]
  * cumulative, cell a*nb+b. */
