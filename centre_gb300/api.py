@@ -97,6 +97,21 @@ class Context:
                                                 _ptr(bins), _ptr(ext)))
         return bins, ext
 
+    def discretize_vmkde(self, data, nmaxconf=5, kappa=1.0, sdo_nstep=5, sdo_conv=1e-4,
+                         sdo_niter=1000):
+        """von Mises KDE conformer bins of torsions [ndof][nframes] ->
+        (bins [ndof][1][nframes], minima [ndof][nmaxconf] rad, nfound [ndof])."""
+        data = _c(data, np.float32)
+        ndof, n = data.shape
+        bins = np.empty((ndof, 1, n), np.uint8)
+        minima = np.zeros((ndof, nmaxconf), np.float64)
+        nfound = np.zeros(ndof, np.uint8)
+        self.check(self.L.centre_gpu_discretize_vmkde(self.h, _ptr(data), ndof, n, int(nmaxconf),
+                                                      float(kappa), int(sdo_nstep),
+                                                      float(sdo_conv), int(sdo_niter),
+                                                      _ptr(bins), _ptr(minima), _ptr(nfound)))
+        return bins, minima, nfound
+
     def entropy1d(self, params: EntropyParams, types, bins, ext, want_freq=False, out=None):
         bins = _c(bins, np.uint8)
         types = _c(types, np.uint8)

@@ -42,7 +42,11 @@ def _compile(src: str, ptxas_verbose: bool) -> tuple[str, str]:
     if (not ptxas_verbose and os.path.exists(obj)
             and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps)):
         return obj, ""
+    # host code without FMA contraction: the host-side double arithmetic that
+    # must match the reference bit for bit (KDE bandwidth, bin thresholds)
+    # then rounds the same on x86-64 and aarch64
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-ffp-contract=off",
            "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-c", os.path.join(CSRC, src),
            "-o", obj]
     if ptxas_verbose:

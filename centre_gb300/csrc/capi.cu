@@ -772,9 +772,33 @@ int centre_gpu_discretize_vmkde(centre_ctx *ctx, const float *data, uint32_t ndo
                                 uint64_t nframes, uint8_t nmaxconf, double kappa,
                                 uint32_t sdo_nstep, double sdo_conv, uint32_t sdo_niter,
                                 uint8_t *bins, double *minima, uint8_t *nfound) {
-  (void)data; (void)ndof; (void)nframes; (void)nmaxconf; (void)kappa; (void)sdo_nstep;
-  (void)sdo_conv; (void)sdo_niter; (void)bins; (void)minima; (void)nfound;
-  return set_error(ctx, CENTRE_E_UNSUPPORTED, "von Mises KDE path not built yet");
+  if (!ctx || !data || !bins || !minima || !nfound)
+    return set_error(ctx, CENTRE_E_ARG, "null argument");
+  if (ndof == 0 || nframes == 0) return CENTRE_OK;
+  cudaSetDevice(ctx->device);
+  int st = CENTRE_OK;
+  const size_t nin = (size_t)ndof * nframes * 4;
+  unsigned char *d_in = (unsigned char *)scratch(ctx, kSlotIn, nin, &st);
+  if (!d_in) return st;
+  uint8_t *d_bins = (uint8_t *)scratch(ctx, kSlotBins, (size_t)ndof * nframes, &st);
+  if (!d_bins) return st;
+  const size_t nw = vmkde_work_doubles(ndof);
+  double *d_work = (double *)scratch(ctx, kSlotAux,
+                                     sizeof(double) * (nw + (size_t)ndof * nmaxconf) + ndof + 16,
+                                     &st);
+  if (!d_work) return st;
+  double *d_min = d_work + nw;
+  uint8_t *d_nf = reinterpret_cast<uint8_t *>(d_min + (size_t)ndof * nmaxconf);
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(d_in, data, nin, cudaMemcpyHostToDevice, ctx->stream));
+  CENTRE_TRY(launch_vmkde(ctx, (const float *)d_in, ndof, nframes, nmaxconf, kappa, sdo_nstep,
+                          sdo_conv, sdo_niter, d_bins, d_min, d_nf, d_work));
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(bins, d_bins, (size_t)ndof * nframes, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(minima, d_min, sizeof(double) * ndof * nmaxconf,
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(nfound, d_nf, ndof, cudaMemcpyDeviceToHost, ctx->stream));
+  CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return CENTRE_OK;
 }
 
 }  // extern "C"

@@ -146,6 +146,13 @@ int launch_discretize(centre_ctx *ctx, int bat_type, const float *d_data, uint32
                       uint64_t nframes, const uint8_t *schemes, uint32_t nschemes,
                       uint8_t bins_ref, int optimize, uint8_t *d_bins, double *d_ext);
 
+// vmkde.cu
+int launch_vmkde(centre_ctx *ctx, const float *d_data, uint32_t ndof, uint64_t nframes,
+                 uint8_t nmaxconf, double kappa, uint32_t sdo_nstep, double sdo_conv,
+                 uint32_t sdo_niter, uint8_t *d_bins, double *d_minima, uint8_t *d_nfound,
+                 double *d_work);
+size_t vmkde_work_doubles(uint32_t ndof);
+
 // pairs_tc.cu
 bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes);
 int launch_pairs_tc(centre_ctx *ctx, const PairParams &P, const double *d_tab, U128 *d_sclnc,

@@ -121,7 +121,11 @@ int centre_gpu_discretize_dev(centre_ctx *ctx, int bat_type, const float *data,
 
 /* von Mises KDE conformer assignment of torsions: Real2Int::getMinimaPositions
  * (src/Real2Int.cpp:481) with analyticGrad=false as Discretizer.cpp:177 calls
- * it.  minima [ndof][nmaxconf] radians, nfound [ndof]. */
+ * it.  minima [ndof][nmaxconf] radians (unused slots 0), nfound [ndof];
+ * bins [ndof][nframes].  The reference records min/max/avg/phase as 1000.0
+ * for KDE-binned DOFs (Discretizer.cpp:139-142).  The grid sums run in FP64
+ * in a different order from the reference, so minima agree to rounding and
+ * a frame lying within rounding of a minimum can take the other label. */
 int centre_gpu_discretize_vmkde(centre_ctx *ctx, const float *data,
                                 uint32_t ndof, uint64_t nframes,
                                 uint8_t nmaxconf, double kappa,

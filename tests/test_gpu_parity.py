@@ -311,3 +311,35 @@ def test_tc_counts_identical_to_atomic(gpu, orc, natoms, nframes, nsteps, nb):
         s_at = gpu.entropy2d(pa, types, bins, ext)
         s_tc = gpu.entropy2d(pt, types, bins, ext)
         assert np.array_equal(s_at, s_tc)
+
+
+# ----------------------------------------------------- von Mises KDE ----
+def _kde_compare(gb, gm, gf, ob, omins, of, x):
+    """Bins equal except frames within rounding of a minimum; minima agree."""
+    assert gf == of
+    np.testing.assert_allclose(gm[:gf], omins, rtol=0, atol=1e-9)
+    diff = np.nonzero(gb != ob)[0]
+    for k in diff:
+        assert np.min(np.abs(np.float64(x[k]) - omins)) < 1e-9, (k, x[k])
+    return len(diff)
+
+
+def test_vmkde_golden_fixture(gpu, golden):
+    g = golden("vmkde_ref.npz")
+    t = g["torsions"]
+    for kappa in (1.0, 8.0):
+        bins, mins, nf = gpu.discretize_vmkde(t, 5, kappa, 5, 1e-4, 1000)
+        for d in range(len(t)):
+            want_b = g[f"k{kappa:g}_d{d}_bins"]
+            want_m = g[f"k{kappa:g}_d{d}_minima"]
+            _kde_compare(bins[d, 0], mins[d], int(nf[d]), want_b, want_m, len(want_m), t[d])
+
+
+@pytest.mark.parametrize("nframes,kappa,nconf", [(20_000, 1.0, 5), (10_007, 8.0, 3), (4_000, 50.0, 9)])
+def test_vmkde_vs_oracle(gpu, orc, nframes, kappa, nconf):
+    tr = chain_trajectory(12, nframes, seed=int(kappa) + nframes)
+    t = tr.torsions
+    bins, mins, nf = gpu.discretize_vmkde(t, nconf, kappa, 5, 1e-4, 1000)
+    for d in range(len(t)):
+        ob, om, of = orc.vmkde(t[d], nconf, kappa, 5, 1e-4, 1000)
+        _kde_compare(bins[d, 0], mins[d], int(nf[d]), ob, om, of, t[d])
