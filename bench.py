@@ -362,6 +362,147 @@ def run_e2e(ctx, tr, args, w, world, dist, dev):
             "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3, "steps": steps}
 
 
+# ----------------------------------------------- batched trajectories ----
+def run_batch(args):
+    """Many trajectories of uneven length scored in one captured graph
+    (centre_gpu_entropy_batch_dev): 1-D and all-pairs joint entropies at 10
+    frame prefixes, MI, MIE-2 and MIST sums per trajectory.  Metric: MI pairs
+    (summed over trajectories) per second of the whole batch."""
+    import torch
+    from centre_gb300.api import Context, make_params
+    from centre_gb300.synth import BATCHES, batch_specs, chain_blocks_torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    b = BATCHES[args.workload]
+    nb, nsteps = b["nbins"], b["nsteps"]
+    ctx = Context(local)
+    stream = torch.cuda.Stream(device=dev)
+    ctx.set_stream(stream.cuda_stream)
+    specs = batch_specs(args.workload, seed=1 + rank)
+    systems, host_bins = [], []
+    tot_pairs = tot_incr = 0
+    with torch.cuda.stream(stream):
+        for natoms, nframes, seed in specs:
+            blocks = chain_blocks_torch(natoms, nframes, seed, dev, coupling=b["coupling"])
+            ndof = sum(x.shape[0] for _, x in blocks)
+            npairs = ndof * (ndof - 1) // 2
+            bins = torch.empty((ndof, 1, nframes), dtype=torch.uint8, device=dev)
+            ext = torch.empty((ndof, 4), dtype=torch.float64, device=dev)
+            off = 0
+            for typ, data in blocks:
+                k = data.shape[0]
+                ctx.discretize_dev(typ, data, [nb], bins[off:off + k], ext[off:off + k])
+                off += k
+            del blocks
+            types = torch.tensor(sum([[t] * k for t, k in ((1, natoms - 1), (2, natoms - 2),
+                                                          (3, natoms - 3))], []),
+                                 dtype=torch.uint8, device=dev)
+            systems.append({"types": types, "bins": bins, "ext": ext,
+                            "s1": torch.empty((ndof, nsteps), dtype=torch.float64, device=dev),
+                            "s2": torch.empty((npairs, nsteps), dtype=torch.float64, device=dev),
+                            "mi": torch.empty((npairs, nsteps), dtype=torch.float64, device=dev)})
+            tot_pairs += npairs
+            tot_incr += npairs * nsteps * (nframes // nsteps)
+    torch.cuda.synchronize(dev)
+    p = make_params(0, nsteps, [nb], [0], True)
+
+    def step():
+        return ctx.entropy_batch_dev(p, systems)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+
+    t0 = time.perf_counter()
+    step()           # tunes the count kernel and captures the graph
+    first_ms = (time.perf_counter() - t0) * 1e3
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    ctx.enable_timing(True)
+    launches0 = ctx.launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            res = step()
+        ev1.record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+    ms = ev0.elapsed_time(ev1)
+    step_ms = max(ms, wall * 1e3) / args.steps
+    launches = ctx.launches - launches0
+    graph_ms, ngraph = ctx.timer(2)
+    ctx.enable_timing(False)
+    t = torch.tensor([step_ms], device=dev)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    step_ms = float(t.item())
+    hbm, bf16, src = peaks()
+    fp8_peak = 2.0 * bf16
+    # tot_incr = sum over chains of pairs x frames used: 2*B^2 one-hot flops each
+    achieved = 2.0 * tot_incr * nb * nb / (step_ms / 1e3) / 1e12
+    ndofs = [3 * a - 6 for a, _, _ in specs]
+    out = {
+        "metric": METRIC, "value": world * tot_pairs / (step_ms / 1e3), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded BAT chains drawn on the device, float32)",
+        "config": {"workload": f"{args.workload}: {len(specs)} chains, {min(ndofs)}..{max(ndofs)} "
+                               f"DOFs, {min(f for _, f, _ in specs)}..{max(f for _, f, _ in specs)} "
+                               f"frames, {nb} bins, {nsteps} prefixes, ML, all pairs "
+                               f"({tot_pairs} in total), MIE-2 + MIST per chain",
+                   "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
+        "first_call_ms": first_ms,
+        "increments_per_s": tot_incr / (step_ms / 1e3),
+        "graph_ms_per_step": graph_ms / max(ngraph, 1),
+        "roofline": {"bound": "tensor", "kernel": "whole batch graph", "achieved": achieved,
+                     "peak": fp8_peak, "unit": "TFLOP/s", "frac": achieved / fp8_peak,
+                     "traffic": None,
+                     "note": f"2*N*B^2 one-hot flops per pair (B={nb}); fp8 peak = 2 x {src} bf16"},
+        "gpu_launches": launches,
+    }
+    clocks = clk.summary()
+    if clocks:
+        out["clocks"] = clocks
+    if not args.no_e2e:
+        # host bins in (pinned), the batch, the sums back on the host
+        pins = [torch.empty(sd["bins"].shape, dtype=torch.uint8, pin_memory=True)
+                for sd in systems]
+        for h, sd in zip(pins, systems):
+            h.copy_(sd["bins"])
+        torch.cuda.synchronize(dev)
+        steps = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                for h, sd in zip(pins, systems):
+                    sd["bins"].copy_(h, non_blocking=True)
+            step()
+        dt = (time.perf_counter() - t0) / steps
+        G = nsteps
+        out["e2e"] = {"value": world * tot_pairs / dt, "unit": UNIT,
+                      "h2d_bytes_per_step": int(sum(h.numel() for h in pins)),
+                      "d2h_bytes_per_step": int(len(systems) * 2 * G * 17 * 8),
+                      "ms_per_step": dt * 1e3, "steps": steps}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
 # ------------------------------------------------------- reference arm ----
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
@@ -412,6 +553,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     args = ap.parse_args()
     global NBINS, NSTEPS
+    from centre_gb300.synth import BATCHES
+    if args.workload in BATCHES:
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "batched workloads are "
+                              "measured against the single-trajectory reference arm"}))
+            return
+        run_batch(args)
+        return
     w = workload(args.workload)
     NBINS, NSTEPS = w["nbins"], w["nsteps"]
     if args.impl == "reference":

@@ -26,6 +26,22 @@ class CentreError(RuntimeError):
         self.status = status
 
 
+class System(C.Structure):
+    """One trajectory of a batch (centre_system)."""
+    _fields_ = [
+        ("ndof", C.c_uint32),
+        ("nframes", C.c_uint64),
+        ("types", C.c_void_p),
+        ("bins", C.c_void_p),
+        ("extremes", C.c_void_p),
+        ("s1", C.c_void_p),
+        ("s2", C.c_void_p),
+        ("mi", C.c_void_p),
+        ("mie_sums", C.c_void_p),
+        ("mist_sums", C.c_void_p),
+    ]
+
+
 class EntropyParams(C.Structure):
     _fields_ = [
         ("nframes", C.c_uint64),
@@ -93,6 +109,8 @@ _SIGS = {
                                    C.c_uint64, _vp, _vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     "centre_gpu_score_dev": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp, _vp,
                                        C.c_uint64, _vp, _vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "centre_gpu_entropy_batch_dev": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32,
+                                               C.POINTER(System)]),
 }
 
 _lib = None

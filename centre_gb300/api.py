@@ -14,6 +14,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import CentreError, EntropyParams, make_params, SUMS_COLS, SUMS_NAMES  # noqa: F401
+from ._lib import System
 
 BOND, ANGLE, DIHEDRAL = 1, 2, 3
 ML, MM, CS, JS = 0, 1, 2, 3
@@ -25,6 +26,11 @@ def _ptr(a):
     if isinstance(a, np.ndarray):
         return a.ctypes.data_as(C.c_void_p)
     return C.c_void_p(int(a.data_ptr()))  # torch tensor
+
+
+def _addr(a):
+    p = _ptr(a)
+    return None if p is None else p.value
 
 
 def _c(a, dt):
@@ -232,3 +238,26 @@ class Context:
                                                int(bool(build_tree)), _ptr(mi_out), _ptr(mie),
                                                _ptr(mist), _ptr(tree), _ptr(ntree)))
         return {"mie": mie, "mist": mist, "tree": [tree[g, : ntree[g]].copy() for g in range(G)]}
+
+    def entropy_batch_dev(self, params, systems, build_tree=True):
+        """Score several trajectories in one captured graph.
+
+        systems: list of dicts with CUDA tensors ``types`` uint8 [ndof],
+        ``bins`` uint8 [ndof][nsch][nframes], ``ext`` f64 [ndof][4] and
+        outputs ``s1`` f64 [ndof][est][sch][steps], ``s2`` f64
+        [npairs][est][sch][steps] (all pairs i<j), optional ``mi`` like s2.
+        Returns per trajectory {"mie": [G][17], "mist": [G][17] or None}.
+        """
+        G = params.nestimators * params.nschemes * params.nsteps
+        arr = (System * len(systems))()
+        keep = []
+        for k, sd in enumerate(systems):
+            ndof, n = int(sd["bins"].shape[0]), int(sd["bins"].shape[2])
+            mie = np.zeros((G, SUMS_COLS), np.float64)
+            mist = np.zeros((G, SUMS_COLS), np.float64) if build_tree else None
+            keep.append((mie, mist))
+            arr[k] = System(ndof, n, *[_addr(x) for x in (
+                sd["types"], sd["bins"], sd["ext"], sd["s1"], sd["s2"], sd.get("mi"), mie, mist)])
+        self.check(self.L.centre_gpu_entropy_batch_dev(self.h, C.byref(params), len(systems),
+                                                       arr))
+        return [{"mie": m, "mist": t} for m, t in keep]

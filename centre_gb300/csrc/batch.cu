@@ -1,0 +1,368 @@
+// batch.cu -- many trajectories of uneven length in one captured graph.
+//
+// The reference scores one trajectory per run (EntropyCalculator::run then
+// EntropyScorer::run, src/EntropyCalculator.cpp:1090, src/EntropyScorer.cpp:7)
+// and its convergence steps are prefixes of the frame axis
+// (src/Estimators.cpp:162-188).  centre_gpu_entropy_batch_dev scores several
+// trajectories at once: their 1-D entropies, one persistent all-pairs count
+// kernel whose CTAs stride through the (trajectory, tile) work list of every
+// trajectory, the entropy finalisation, and the MI / MIE / MIST scoring with
+// a fixed number of Boruvka rounds, all enqueued without host
+// synchronisation and captured into one CUDA graph.  The graph is cached and
+// replayed when the same batch (same buffers, sizes and parameters) comes
+// back.  The count kernel's tile shape and block size are chosen by timing the
+// candidates on a sample of the real work list (autotuning), once per
+// (bins, steps, schemes) combination per context.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "entropy.cuh"
+
+namespace centre {
+namespace {
+
+struct TuneKey {
+  int nb, nsteps, nschemes;
+};
+struct TuneVal {
+  int tile, threads, blocks_per_sm;
+};
+
+struct BatchCache {
+  std::vector<unsigned char> key;     // bytes of the call's arguments
+  cudaGraphExec_t exec = nullptr;
+  uint64_t nodes = 0;
+  void *base = nullptr;               // scratch the graph was captured on
+  void *h_stage = nullptr;            // pinned MIE/MIST rows
+  size_t stage_bytes = 0;
+  BatchSys *h_sys = nullptr;          // pinned work list, copied in by the graph
+  size_t sys_cap = 0;
+};
+
+// per-context state kept across calls (tuning results, cached graph)
+struct BatchState {
+  std::vector<std::pair<TuneKey, TuneVal>> tuned;
+  BatchCache cache;
+};
+
+BatchState &state_of(centre_ctx *ctx) {
+  if (!ctx->batch_state) ctx->batch_state = new BatchState();
+  return *reinterpret_cast<BatchState *>(ctx->batch_state);
+}
+
+size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
+
+int tiles_fitting(int nb) {
+  // square tiles whose histograms fit the shared-memory budget
+  const int w = pair_tile_for(nb);
+  int t = 1;
+  while ((t + 1) * (t + 1) <= w && t < 4) ++t;
+  return t;
+}
+
+}  // namespace
+
+void batch_state_free(centre_ctx *ctx) {
+  if (!ctx->batch_state) return;
+  BatchState *st = reinterpret_cast<BatchState *>(ctx->batch_state);
+  if (st->cache.exec) cudaGraphExecDestroy(st->cache.exec);
+  if (st->cache.h_stage) cudaFreeHost(st->cache.h_stage);
+  if (st->cache.h_sys) cudaFreeHost(st->cache.h_sys);
+  delete st;
+  ctx->batch_state = nullptr;
+}
+
+}  // namespace centre
+
+using namespace centre;
+
+extern "C" int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entropy_params *p,
+                                            uint32_t nsys, const centre_system *sys) {
+  if (!ctx || !p || (nsys && !sys)) return set_error(ctx, CENTRE_E_ARG, "null argument");
+  if (nsys == 0) return CENTRE_OK;
+  cudaSetDevice(ctx->device);
+  if (p->nsteps == 0 || p->nschemes == 0 || p->nschemes > kMaxSchemes || p->nestimators == 0 ||
+      p->nestimators > 4)
+    return set_error(ctx, CENTRE_E_ARG, "bad entropy parameters");
+  for (int e = 0; e < p->nestimators; ++e)
+    if (p->estimators[e] > CENTRE_MM)
+      return set_error(ctx, CENTRE_E_UNSUPPORTED, "batch supports the ML and MM estimators");
+  int nbmax = 0;
+  for (int s = 0; s < p->nschemes; ++s) {
+    if (p->bin_schemes[s] == 0 || pair_tile_for(p->bin_schemes[s]) < 1)
+      return set_error(ctx, CENTRE_E_UNSUPPORTED, "bin count too large for shared-memory counts");
+    nbmax = std::max(nbmax, (int)p->bin_schemes[s]);
+  }
+  for (uint32_t k = 0; k < nsys; ++k) {
+    const centre_system &S = sys[k];
+    if (S.ndof < 2 || S.nframes < p->nsteps || S.nframes > kMaxFrames || !S.types || !S.bins ||
+        !S.extremes || !S.s1 || !S.s2 || !S.mie_sums)
+      return set_error(ctx, CENTRE_E_ARG, "bad trajectory in batch");
+  }
+  const int G = p->nestimators * p->nschemes * p->nsteps;
+  if (G > 256) return set_error(ctx, CENTRE_E_UNSUPPORTED, "estimators*schemes*steps must be <= 256");
+  BatchState &bs = state_of(ctx);
+
+  // ---- per-trajectory parameters and scratch layout ----------------------
+  std::vector<EntParams> E(nsys);
+  std::vector<ScoreParams> SP(nsys);
+  std::vector<unsigned char> types_key;   // DOF types are part of the cache key
+  std::vector<size_t> off_l(nsys), off_m(nsys), off_z(nsys), off_w(nsys), off_sc(nsys),
+      off_mi(nsys), off_mie(nsys), off_mist(nsys);
+  size_t total = 0;
+  for (uint32_t k = 0; k < nsys; ++k) {
+    const centre_system &S = sys[k];
+    EntParams &e = E[k];
+    memset(&e, 0, sizeof(e));
+    e.nframes = S.nframes;
+    e.step_size = S.nframes / p->nsteps;
+    e.nsteps = p->nsteps;
+    e.nschemes = p->nschemes;
+    e.nests = p->nestimators;
+    e.jacobian = p->jacobian ? 1 : 0;
+    e.kde = p->kde ? 1 : 0;
+    int off = 0;
+    for (int s = 0; s < p->nschemes; ++s) {
+      e.schemes[s] = p->bin_schemes[s];
+      e.scheme_off[s] = off;
+      off += p->bin_schemes[s];
+    }
+    e.nbins_sum = off;
+    for (int q = 0; q < p->nestimators; ++q) e.ests[q] = p->estimators[q];
+    const uint64_t npairs = (uint64_t)S.ndof * (S.ndof - 1) / 2;
+    ScoreParams &sp = SP[k];
+    memset(&sp, 0, sizeof(sp));
+    sp.ndof = S.ndof;
+    sp.npairs = npairs;
+    sp.G = G;
+    sp.all_pairs = 1;
+    sp.sorted_types = 1;   // trajectories list bonds, angles, torsions in order
+    std::vector<uint8_t> ht(S.ndof);
+    CENTRE_CUDA(ctx, cudaMemcpy(ht.data(), S.types, S.ndof, cudaMemcpyDeviceToHost));
+    for (uint32_t d = 0; d < S.ndof; ++d) {
+      const int t = ht[d];
+      if (t < 1 || t > 3) return set_error(ctx, CENTRE_E_ARG, "DOF type must be 1, 2 or 3");
+      if (d > 0 && t < ht[d - 1]) sp.sorted_types = 0;
+      if (sp.type_count[t] == 0) sp.type_start[t] = d;
+      sp.type_count[t]++;
+    }
+    types_key.insert(types_key.end(), ht.begin(), ht.end());
+    off_l[k] = total;
+    total += align256(sizeof(double) * S.ndof * p->nschemes * p->nsteps);
+    off_m[k] = total;
+    total += align256(sizeof(U128) * npairs * p->nsteps);
+    off_z[k] = total;
+    total += align256(sizeof(unsigned) * npairs * p->nsteps);
+    off_w[k] = total;
+    total += align256(sizeof(double) * ((uint64_t)S.ndof * p->nschemes + p->nsteps));
+    off_sc[k] = total;
+    total += align256(score_scratch_bytes(sp, S.mist_sums != nullptr));
+    off_mi[k] = total;
+    total += S.mi ? 0 : align256(sizeof(double) * npairs * G);
+    off_mie[k] = total;
+    total += align256(sizeof(double) * G * CENTRE_SUMS_COLS);
+    off_mist[k] = total;
+    total += align256(sizeof(double) * G * CENTRE_SUMS_COLS);
+  }
+  const size_t sys_off = total;
+  total += align256(sizeof(BatchSys) * nsys * 4);   // up to 4 tile variants
+  int st = CENTRE_OK;
+  unsigned char *base = (unsigned char *)scratch(ctx, kSlotMoments, total, &st);
+  if (!base) return st;
+
+  // ---- work lists for a tile shape ---------------------------------------
+  auto build_sys = [&](int tile, std::vector<BatchSys> &out) -> uint64_t {
+    out.resize(nsys);
+    uint64_t items = 0;
+    for (uint32_t k = 0; k < nsys; ++k) {
+      BatchSys &b = out[k];
+      b.bins = sys[k].bins;
+      b.nframes = sys[k].nframes;
+      b.step_size = E[k].step_size;
+      b.ndof = sys[k].ndof;
+      b.ntile = (sys[k].ndof + tile - 1) / tile;
+      b.item_begin = items;
+      b.sclnc = reinterpret_cast<U128 *>(base + off_m[k]);
+      b.nnz = reinterpret_cast<unsigned *>(base + off_z[k]);
+      items += b.ntile * (b.ntile + 1) / 2;
+    }
+    return items;
+  };
+
+  // ---- autotune tile shape x block size (once per key) -------------------
+  TuneKey key{nbmax, p->nsteps, p->nschemes};
+  TuneVal best{0, 0, 0};
+  for (auto &kv : bs.tuned)
+    if (kv.first.nb == key.nb && kv.first.nsteps == key.nsteps && kv.first.nschemes == key.nschemes)
+      best = kv.second;
+  const bool was_timing = ctx->timing;
+  ctx->timing = false;
+  if (best.tile == 0) {
+    const int tmax = tiles_fitting(nbmax);
+    float best_per = 0.f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int vi = 0;
+    for (int tile = tmax; tile >= std::max(1, tmax - 2); --tile, ++vi) {
+      std::vector<BatchSys> bsys;
+      const uint64_t items = build_sys(tile, bsys);
+      BatchSys *d_sys = reinterpret_cast<BatchSys *>(base + sys_off) + (size_t)vi * nsys;
+      CENTRE_CUDA(ctx, cudaMemcpyAsync(d_sys, bsys.data(), sizeof(BatchSys) * nsys,
+                                       cudaMemcpyHostToDevice, ctx->stream));
+      CENTRE_TRY(prepare_pairs_hist_batch(ctx, tile, nbmax));
+      for (int threads : {256, 512}) {
+        int per_sm = 0;
+        CENTRE_TRY(pairs_hist_batch_occupancy(ctx, tile, threads, nbmax, &per_sm));
+        if (per_sm < 1) continue;
+        const int grid = ctx->sm_count * per_sm;
+        const uint64_t sample = std::min<uint64_t>(items, (uint64_t)grid * 2);
+        BatchCommon B;
+        B.item0 = 0;
+        B.nsteps = p->nsteps;
+        B.nschemes = p->nschemes;
+        B.scheme = 0;
+        B.nb = p->bin_schemes[0];
+        CENTRE_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+        CENTRE_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        CENTRE_TRY(launch_pairs_hist_batch(ctx, d_sys, (int)nsys, sample, B, tile, threads,
+                                           (int)std::min<uint64_t>(grid, sample),
+                                           (const double *)ctx->d_clnc));
+        CENTRE_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        CENTRE_CUDA(ctx, cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        // pairs per tile grows as tile^2: compare time per pair
+        const float per = ms / (float)(sample * tile * tile);
+        if (best.tile == 0 || per < best_per) {
+          best_per = per;
+          best = TuneVal{tile, threads, per_sm};
+        }
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    bs.tuned.push_back({key, best});
+  }
+
+  // ---- the call's key: replay the cached graph when it matches -----------
+  std::vector<unsigned char> ck(sizeof(centre_entropy_params) + sizeof(centre_system) * nsys);
+  memcpy(ck.data(), p, sizeof(centre_entropy_params));
+  memcpy(ck.data() + sizeof(centre_entropy_params), sys, sizeof(centre_system) * nsys);
+  ck.insert(ck.end(), types_key.begin(), types_key.end());
+  ck.push_back((unsigned char)best.tile);
+  const size_t stage_bytes = sizeof(double) * G * CENTRE_SUMS_COLS * 2 * nsys;
+  BatchCache &C = bs.cache;
+  if (!(C.exec && C.key == ck && C.base == (void *)base)) {
+    if (C.exec) {
+      cudaGraphExecDestroy(C.exec);
+      C.exec = nullptr;
+    }
+    if (C.stage_bytes < stage_bytes) {
+      if (C.h_stage) cudaFreeHost(C.h_stage);
+      C.h_stage = nullptr;
+      C.stage_bytes = 0;
+      CENTRE_CUDA(ctx, cudaMallocHost(&C.h_stage, stage_bytes));
+      C.stage_bytes = stage_bytes;
+    }
+    if (C.sys_cap < nsys) {
+      if (C.h_sys) cudaFreeHost(C.h_sys);
+      C.h_sys = nullptr;
+      C.sys_cap = 0;
+      CENTRE_CUDA(ctx, cudaMallocHost(&C.h_sys, sizeof(BatchSys) * nsys));
+      C.sys_cap = nsys;
+    }
+    std::vector<BatchSys> bsys;
+    const uint64_t items = build_sys(best.tile, bsys);
+    memcpy(C.h_sys, bsys.data(), sizeof(BatchSys) * nsys);
+    BatchSys *d_sys = reinterpret_cast<BatchSys *>(base + sys_off);
+    CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    // the count kernel's shared-memory limit is set outside the capture
+    CENTRE_TRY(prepare_pairs_hist_batch(ctx, best.tile, nbmax));
+    const uint64_t launches0 = ctx->launches;
+    CENTRE_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = CENTRE_OK;
+    int *d_flag = ctx->d_flag;
+    do {
+      if (cudaMemsetAsync(d_flag, 0, sizeof(int), ctx->stream) != cudaSuccess ||
+          cudaMemcpyAsync(d_sys, C.h_sys, sizeof(BatchSys) * nsys, cudaMemcpyHostToDevice,
+                          ctx->stream) != cudaSuccess) {
+        rc = CENTRE_E_CUDA;
+        break;
+      }
+      for (uint32_t k = 0; k < nsys && rc == CENTRE_OK; ++k)
+        rc = launch_entropy1d(ctx, E[k], sys[k].ndof, sys[k].types, sys[k].bins, sys[k].extremes,
+                              sys[k].s1, nullptr, reinterpret_cast<double *>(base + off_l[k]));
+      for (int s = 0; s < p->nschemes && rc == CENTRE_OK; ++s) {
+        BatchCommon B;
+        B.item0 = 0;
+        B.nsteps = p->nsteps;
+        B.nschemes = p->nschemes;
+        B.scheme = s;
+        B.nb = p->bin_schemes[s];
+        const int grid = (int)std::min<uint64_t>(items, (uint64_t)ctx->sm_count * best.blocks_per_sm);
+        rc = launch_pairs_hist_batch(ctx, d_sys, (int)nsys, items, B, best.tile, best.threads,
+                                     grid, (const double *)ctx->d_clnc);
+        for (uint32_t k = 0; k < nsys && rc == CENTRE_OK; ++k) {
+          const uint64_t npairs = (uint64_t)sys[k].ndof * (sys[k].ndof - 1) / 2;
+          rc = launch_finalize2d_into(ctx, E[k], s, sys[k].ndof, sys[k].extremes,
+                                      reinterpret_cast<double *>(base + off_l[k]),
+                                      reinterpret_cast<U128 *>(base + off_m[k]),
+                                      reinterpret_cast<unsigned *>(base + off_z[k]), npairs,
+                                      reinterpret_cast<double *>(base + off_w[k]), sys[k].s2);
+        }
+      }
+      for (uint32_t k = 0; k < nsys && rc == CENTRE_OK; ++k) {
+        double *mi = sys[k].mi ? sys[k].mi : reinterpret_cast<double *>(base + off_mi[k]);
+        double *d_mie = reinterpret_cast<double *>(base + off_mie[k]);
+        double *d_mist = sys[k].mist_sums ? reinterpret_cast<double *>(base + off_mist[k]) : nullptr;
+        rc = launch_score_async(ctx, SP[k], sys[k].types, nullptr, sys[k].s1, sys[k].s2, mi, d_mie,
+                                d_mist, base + off_sc[k]);
+        if (rc != CENTRE_OK) break;
+        double *h = reinterpret_cast<double *>(C.h_stage) + (size_t)k * G * CENTRE_SUMS_COLS * 2;
+        if (cudaMemcpyAsync(h, d_mie, sizeof(double) * G * CENTRE_SUMS_COLS, cudaMemcpyDeviceToHost,
+                            ctx->stream) != cudaSuccess) { rc = CENTRE_E_CUDA; break; }
+        if (d_mist && cudaMemcpyAsync(h + G * CENTRE_SUMS_COLS, d_mist,
+                                      sizeof(double) * G * CENTRE_SUMS_COLS,
+                                      cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess) {
+          rc = CENTRE_E_CUDA;
+          break;
+        }
+      }
+    } while (false);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+    if (rc != CENTRE_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      ctx->timing = was_timing;
+      return rc;
+    }
+    CENTRE_CUDA(ctx, ce);
+    C.nodes = ctx->launches - launches0;
+    const cudaError_t ie = cudaGraphInstantiate(&C.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    ctx->launches = launches0;
+    CENTRE_CUDA(ctx, ie);
+    C.key = ck;
+    C.base = base;
+  }
+  ctx->timing = was_timing;
+  {
+    KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
+    CENTRE_CUDA(ctx, cudaGraphLaunch(C.exec, ctx->stream));
+  }
+  ctx->launches += C.nodes;
+  CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  int flag = 0;
+  CENTRE_CUDA(ctx, cudaMemcpy(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag & kFlagBinRange) return set_error(ctx, CENTRE_E_BINRANGE, "bin index >= bin count");
+  for (uint32_t k = 0; k < nsys; ++k) {
+    const double *h = reinterpret_cast<const double *>(C.h_stage) + (size_t)k * G * CENTRE_SUMS_COLS * 2;
+    memcpy(sys[k].mie_sums, h, sizeof(double) * G * CENTRE_SUMS_COLS);
+    if (sys[k].mist_sums)
+      memcpy(sys[k].mist_sums, h + G * CENTRE_SUMS_COLS, sizeof(double) * G * CENTRE_SUMS_COLS);
+  }
+  return CENTRE_OK;
+}

@@ -51,6 +51,7 @@ struct centre_ctx {
   std::vector<cudaEvent_t> event_pool;
   double timer_ms[4] = {0, 0, 0, 0};
   uint64_t timer_n[4] = {0, 0, 0, 0};
+  void *batch_state = nullptr;  // tuned tiles and the cached batch graph
 };
 
 namespace centre {
@@ -71,6 +72,7 @@ int set_error(centre_ctx *ctx, int status, const std::string &msg);
 int check_cuda(centre_ctx *ctx, cudaError_t e, const char *what);
 void *scratch(centre_ctx *ctx, int slot, size_t bytes, int *status);
 void *ctx_clnc(centre_ctx *ctx);
+void batch_state_free(centre_ctx *ctx);
 
 // Scoped event timer around a launch on the context's stream (no-op unless
 // timing is enabled).

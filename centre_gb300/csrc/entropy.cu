@@ -234,60 +234,60 @@ __device__ __noinline__ U128 clnc_far_u128(const double *__restrict__ gtab, unsi
   return u128_from_double((c < (unsigned)kTabGlobal) ? __ldg(gtab + c) : clnc_value(c));
 }
 
-template <int R, int C, bool kCounts>
-__global__ void __launch_bounds__(512)
-pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__ tasks,
-                  const __grid_constant__ PairParams P, const double *__restrict__ gtab,
-                  U128 *__restrict__ sclnc, unsigned *__restrict__ nnz,
-                  unsigned *__restrict__ counts, int *__restrict__ flag) {
-  constexpr int NP = R * C;
-  extern __shared__ __align__(16) unsigned char dyn[];
-  const int nb = P.nb, nb2 = nb * nb;
-  unsigned *hist = reinterpret_cast<unsigned *>(dyn);
-  U128 *tab = reinterpret_cast<U128 *>(dyn + (((size_t)NP * nb2 * 4 + 15) & ~size_t(15)));
-  __shared__ uint32_t rows_s[R], cols_s[C];
-  __shared__ uint64_t out_s[NP];
-  const int tid = threadIdx.x;
-  const uint64_t n = P.nframes;
+// One R x C tile of pairs of one trajectory.
+struct HistJob {
+  const uint8_t *bins;
+  uint64_t nframes;
+  uint64_t step_size;
+  int nsteps;
+  int nschemes;
+  int scheme;
+  int nb;
+  U128 *sclnc;
+  unsigned *nnz;
+  unsigned *counts;
+};
 
-  if (tid == 0) {
-    if (P.all_pairs) {
-      // implicit upper-triangular grid of R x R tiles (R == C)
-      const uint64_t T = P.ntile;
-      uint64_t id = blockIdx.x, bi = 0;
-      while (true) {
-        const uint64_t rowlen = T - bi;
-        if (id < rowlen) break;
-        id -= rowlen;
-        ++bi;
-      }
-      const uint64_t bj = bi + id;
-      for (int r = 0; r < R; ++r) {
-        const uint64_t i = bi * R + r;
-        rows_s[r] = (uint32_t)(i < P.ndof ? i : bi * R);
-      }
-      for (int c = 0; c < C; ++c) {
-        const uint64_t j = bj * C + c;
-        cols_s[c] = (uint32_t)(j < P.ndof ? j : bj * C);
-      }
-      for (int r = 0; r < R; ++r)
-        for (int c = 0; c < C; ++c) {
-          const uint64_t i = bi * R + r, j = bj * C + c;
-          out_s[r * C + c] = (i < j && j < P.ndof) ? tri_index(i, j, P.ndof) : ~0ull;
-        }
-    } else {
-      const PairTask &tk = tasks[blockIdx.x];
-      for (int r = 0; r < R; ++r) rows_s[r] = tk.rows[r < tk.nr ? r : 0];
-      for (int c = 0; c < C; ++c) cols_s[c] = tk.cols[c < tk.nc ? c : 0];
-      for (int r = 0; r < R; ++r)
-        for (int c = 0; c < C; ++c)
-          out_s[r * C + c] = (r < tk.nr && c < tk.nc) ? tk.out[r * tk.nc + c] : ~0ull;
-    }
+// Fill rows/cols/outputs of the all-pairs tile `id` of an upper-triangular
+// grid of R x R tiles over ndof DOFs (thread 0).
+template <int R>
+__device__ void decode_all_pairs_tile(uint64_t id, uint64_t ntile, uint32_t ndof, uint32_t *rows,
+                                      uint32_t *cols, uint64_t *outs) {
+  uint64_t bi = 0;
+  while (true) {
+    const uint64_t rowlen = ntile - bi;
+    if (id < rowlen) break;
+    id -= rowlen;
+    ++bi;
   }
-  for (int i = tid; i < kTabHist; i += blockDim.x) tab[i] = u128_from_double(__ldg(gtab + i));
-  for (int i = tid; i < NP * nb2; i += blockDim.x) hist[i] = 0;
-  __syncthreads();
+  const uint64_t bj = bi + id;
+  for (int r = 0; r < R; ++r) {
+    const uint64_t i = bi * R + r;
+    rows[r] = (uint32_t)(i < ndof ? i : bi * R);
+  }
+  for (int c = 0; c < R; ++c) {
+    const uint64_t j = bj * R + c;
+    cols[c] = (uint32_t)(j < ndof ? j : bj * R);
+  }
+  for (int r = 0; r < R; ++r)
+    for (int c = 0; c < R; ++c) {
+      const uint64_t i = bi * R + r, j = bj * R + c;
+      outs[r * R + c] = (i < j && j < ndof) ? tri_index(i, j, ndof) : ~0ull;
+    }
+}
 
+// Count all frames of one tile and emit its moments (or counts) per step.
+// `hist` is zeroed on entry and left zeroed.  Returns non-zero if a bin was
+// out of range.  All threads of the CTA call it.
+template <int R, int C, bool kCounts>
+__device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_t *cols_s,
+                         const uint64_t *out_s, unsigned *hist, const U128 *tab,
+                         const double *__restrict__ gtab) {
+  constexpr int NP = R * C;
+  const int tid = threadIdx.x;
+  const int nb = J.nb, nb2 = nb * nb;
+  const uint64_t n = J.nframes;
+  const uint8_t *bins = J.bins;
   const uint32_t hist_s = (uint32_t)__cvta_generic_to_shared(hist);
   // DOF rows as 32-bit word offsets (row starts are 4-byte aligned when the
   // word path is used; the byte path rebuilds the byte offset)
@@ -296,12 +296,12 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
   uint32_t rconst[R], cconst[C];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    rw0[r] = (uint32_t)((((uint64_t)rows_s[r] * P.nschemes + P.scheme) * n) >> 2);
+    rw0[r] = (uint32_t)((((uint64_t)rows_s[r] * J.nschemes + J.scheme) * n) >> 2);
     rconst[r] = hist_s + 4u * (uint32_t)(r * C * nb2);
   }
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    cw0[c] = (uint32_t)((((uint64_t)cols_s[c] * P.nschemes + P.scheme) * n) >> 2);
+    cw0[c] = (uint32_t)((((uint64_t)cols_s[c] * J.nschemes + J.scheme) * n) >> 2);
     cconst[c] = 4u * (uint32_t)(c * nb2);
   }
   const uint32_t nb4 = 4u * (uint32_t)nb;
@@ -314,12 +314,12 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
     bool ok = true;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      a[r] = bins[((uint64_t)rows_s[r] * P.nschemes + P.scheme) * n + f];
+      a[r] = bins[((uint64_t)rows_s[r] * J.nschemes + J.scheme) * n + f];
       ok &= a[r] < (uint32_t)nb;
     }
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-      b[c] = bins[((uint64_t)cols_s[c] * P.nschemes + P.scheme) * n + f];
+      b[c] = bins[((uint64_t)cols_s[c] * J.nschemes + J.scheme) * n + f];
       ok &= b[c] < (uint32_t)nb;
     }
     if (!ok) {
@@ -332,8 +332,8 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
       for (int c = 0; c < C; ++c) red_shared_inc(rconst[r] + a[r] * nb4 + cconst[c] + 4u * b[c]);
   };
 
-  for (int t = 0; t < P.nsteps; ++t) {
-    const uint64_t f0 = (uint64_t)t * P.step_size, f1 = f0 + P.step_size;
+  for (int t = 0; t < J.nsteps; ++t) {
+    const uint64_t f0 = (uint64_t)t * J.step_size, f1 = f0 + J.step_size;
     if (word) {
       const uint64_t g0 = (f0 + 3) >> 2, g1 = f1 >> 2;   // whole 4-frame groups
       for (uint64_t f = f0 + tid; f < min(f1, g0 << 2); f += blockDim.x) one_frame(f);
@@ -376,7 +376,7 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
       for (int q = 0; q < NP; ++q) {
         const uint64_t o = out_s[q];
         if (o == ~0ull) continue;
-        unsigned *dst = counts + (o * P.nsteps + t) * (uint64_t)nb2;
+        unsigned *dst = J.counts + (o * J.nsteps + t) * (uint64_t)nb2;
         for (int i = tid; i < nb2; i += blockDim.x) dst[i] = hist[q * nb2 + i];
       }
     } else {
@@ -400,16 +400,114 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
           cz += __shfl_xor_sync(0xffffffffu, cz, off);
         }
         if (lane == 0) {
-          sclnc[o * P.nsteps + t] = acc;
-          nnz[o * P.nsteps + t] = cz;
+          J.sclnc[o * J.nsteps + t] = acc;
+          J.nnz[o * J.nsteps + t] = cz;
         }
       }
     }
     __syncthreads();
   }
-  if (__syncthreads_or(bad) && tid == 0) atomicOr(flag, kFlagBinRange);
+  // leave the histograms zeroed for the next tile of a persistent CTA
+  for (int i = tid; i < NP * nb2; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  return bad;
 }
 
+template <int R, int C, bool kCounts>
+__global__ void __launch_bounds__(512)
+pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__ tasks,
+                  const __grid_constant__ PairParams P, const double *__restrict__ gtab,
+                  U128 *__restrict__ sclnc, unsigned *__restrict__ nnz,
+                  unsigned *__restrict__ counts, int *__restrict__ flag) {
+  constexpr int NP = R * C;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  const int nb2 = P.nb * P.nb;
+  unsigned *hist = reinterpret_cast<unsigned *>(dyn);
+  U128 *tab = reinterpret_cast<U128 *>(dyn + (((size_t)NP * nb2 * 4 + 15) & ~size_t(15)));
+  __shared__ uint32_t rows_s[R], cols_s[C];
+  __shared__ uint64_t out_s[NP];
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    if (P.all_pairs) {
+      decode_all_pairs_tile<R>(blockIdx.x, P.ntile, P.ndof, rows_s, cols_s, out_s);
+    } else {
+      const PairTask &tk = tasks[blockIdx.x];
+      for (int r = 0; r < R; ++r) rows_s[r] = tk.rows[r < tk.nr ? r : 0];
+      for (int c = 0; c < C; ++c) cols_s[c] = tk.cols[c < tk.nc ? c : 0];
+      for (int r = 0; r < R; ++r)
+        for (int c = 0; c < C; ++c)
+          out_s[r * C + c] = (r < tk.nr && c < tk.nc) ? tk.out[r * tk.nc + c] : ~0ull;
+    }
+  }
+  for (int i = tid; i < kTabHist; i += blockDim.x) tab[i] = u128_from_double(__ldg(gtab + i));
+  for (int i = tid; i < NP * nb2; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  HistJob J;
+  J.bins = bins;
+  J.nframes = P.nframes;
+  J.step_size = P.step_size;
+  J.nsteps = P.nsteps;
+  J.nschemes = P.nschemes;
+  J.scheme = P.scheme;
+  J.nb = P.nb;
+  J.sclnc = sclnc;
+  J.nnz = nnz;
+  J.counts = counts;
+  const int bad = hist_tile<R, C, kCounts>(J, rows_s, cols_s, out_s, hist, tab, gtab);
+  if (bad && tid == 0) atomicOr(flag, kFlagBinRange);
+}
+
+// Persistent all-pairs histogram counts over several trajectories: the work
+// list is every (trajectory, tile) pair; CTAs stride through it.
+template <int R>
+__global__ void __launch_bounds__(512)
+pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nitems,
+                        const __grid_constant__ BatchCommon B, const double *__restrict__ gtab,
+                        int *__restrict__ flag) {
+  constexpr int NP = R * R;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  const int nb2 = B.nb * B.nb;
+  unsigned *hist = reinterpret_cast<unsigned *>(dyn);
+  U128 *tab = reinterpret_cast<U128 *>(dyn + (((size_t)NP * nb2 * 4 + 15) & ~size_t(15)));
+  __shared__ uint32_t rows_s[R], cols_s[R];
+  __shared__ uint64_t out_s[NP];
+  __shared__ int sys_s;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kTabHist; i += blockDim.x) tab[i] = u128_from_double(__ldg(gtab + i));
+  for (int i = tid; i < NP * nb2; i += blockDim.x) hist[i] = 0;
+  int bad = 0;
+  for (uint64_t item = blockIdx.x + B.item0; item < nitems; item += gridDim.x) {
+    __syncthreads();
+    if (tid == 0) {
+      int lo = 0, hi = nsys - 1;   // last trajectory whose first item <= item
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sys[mid].item_begin <= item) lo = mid; else hi = mid - 1;
+      }
+      const int s = lo;
+      sys_s = s;
+      decode_all_pairs_tile<R>(item - sys[s].item_begin, sys[s].ntile, sys[s].ndof, rows_s,
+                               cols_s, out_s);
+    }
+    __syncthreads();
+    const BatchSys &S = sys[sys_s];
+    HistJob J;
+    J.bins = S.bins;
+    J.nframes = S.nframes;
+    J.step_size = S.step_size;
+    J.nsteps = B.nsteps;
+    J.nschemes = B.nschemes;
+    J.scheme = B.scheme;
+    J.nb = B.nb;
+    J.sclnc = S.sclnc;
+    J.nnz = S.nnz;
+    J.counts = nullptr;
+    bad |= hist_tile<R, R, false>(J, rows_s, cols_s, out_s, hist, tab, gtab);
+  }
+  if (bad) atomicOr(flag, kFlagBinRange);
+}
+
+// ----------------------------------------------------------------------------
 // ----------------------------------------------------------------------------
 // S2 from the integer moments (ML, MM).  One thread per (pair, step) of a
 // scheme.
@@ -614,6 +712,56 @@ static int launch_hist(centre_ctx *ctx, const PairParams &P, const PairTask *d_t
     pairs_hist_kernel<R, C, false><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
         P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
   }
+  return CENTRE_OK;
+}
+
+// Sets the dynamic shared-memory limit of the batch kernel for tiles of
+// tile x tile pairs with up to nb bins (outside any stream capture).
+int prepare_pairs_hist_batch(centre_ctx *ctx, int tile, int nb) {
+  const size_t smem = (((size_t)tile * tile * nb * nb * 4 + 15) & ~size_t(15)) + 16 * kTabHist;
+  auto set = [&](auto kern) {
+    return check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem), "batch smem attribute");
+  };
+  switch (tile) {
+    case 4: return set(pairs_hist_batch_kernel<4>);
+    case 3: return set(pairs_hist_batch_kernel<3>);
+    case 2: return set(pairs_hist_batch_kernel<2>);
+    default: return set(pairs_hist_batch_kernel<1>);
+  }
+}
+
+size_t pairs_hist_batch_smem(int tile, int nb) {
+  return (((size_t)tile * tile * nb * nb * 4 + 15) & ~size_t(15)) + 16 * kTabHist;
+}
+
+// Resident CTAs per SM of the batch kernel for a tile shape and block size.
+int pairs_hist_batch_occupancy(centre_ctx *ctx, int tile, int threads, int nb, int *per_sm) {
+  const size_t smem = pairs_hist_batch_smem(tile, nb);
+  cudaError_t e;
+  switch (tile) {
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, pairs_hist_batch_kernel<4>, threads, smem); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, pairs_hist_batch_kernel<3>, threads, smem); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, pairs_hist_batch_kernel<2>, threads, smem); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, pairs_hist_batch_kernel<1>, threads, smem); break;
+  }
+  return check_cuda(ctx, e, "batch occupancy");
+}
+
+int launch_pairs_hist_batch(centre_ctx *ctx, const BatchSys *d_sys, int nsys, uint64_t nitems,
+                            const BatchCommon &B, int tile, int threads, int grid,
+                            const double *d_tab) {
+  if (nitems <= B.item0 || grid <= 0) return CENTRE_OK;
+  KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
+  const size_t smem = pairs_hist_batch_smem(tile, B.nb);
+  switch (tile) {
+    case 4: pairs_hist_batch_kernel<4><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_tab, ctx->d_flag); break;
+    case 3: pairs_hist_batch_kernel<3><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_tab, ctx->d_flag); break;
+    case 2: pairs_hist_batch_kernel<2><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_tab, ctx->d_flag); break;
+    default: pairs_hist_batch_kernel<1><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_tab, ctx->d_flag); break;
+  }
+  ctx->launches++;
+  CENTRE_CUDA(ctx, cudaGetLastError());
   return CENTRE_OK;
 }
 

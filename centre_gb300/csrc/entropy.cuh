@@ -31,6 +31,31 @@ struct PairTask {
   uint8_t nr, nc;
 };
 
+// Unsigned 128-bit accumulator for the per-cell c ln c terms.
+struct __align__(16) U128 {
+  unsigned long long lo, hi;
+};
+
+// One trajectory of a batch (device copy; see batch.cu).
+struct BatchSys {
+  const uint8_t *bins;
+  uint64_t nframes;
+  uint64_t step_size;
+  uint64_t ntile;        // tiles per side of the all-pairs grid
+  uint64_t item_begin;   // first work item of this trajectory
+  uint32_t ndof;
+  U128 *sclnc;
+  unsigned *nnz;
+};
+
+struct BatchCommon {
+  uint64_t item0;        // first item to process (autotuning samples)
+  int nsteps;
+  int nschemes;
+  int scheme;
+  int nb;
+};
+
 struct PairParams {
   const uint8_t *bins;
   uint64_t nframes;
@@ -47,11 +72,6 @@ struct PairParams {
 
 constexpr int kTabSmem = 1024;      // c ln c entries kept in shared memory
 constexpr int kTabGlobal = 1 << 16; // entries in the global table
-
-// Unsigned 128-bit accumulator for the per-cell c ln c terms.
-struct __align__(16) U128 {
-  unsigned long long lo, hi;
-};
 
 __device__ __forceinline__ U128 u128_add(U128 a, U128 b) {
   U128 r;
@@ -128,6 +148,12 @@ int pair_tile_for(int nb);
 int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
                         uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
                         unsigned *d_counts);
+int prepare_pairs_hist_batch(centre_ctx *ctx, int tile, int nb);
+size_t pairs_hist_batch_smem(int tile, int nb);
+int pairs_hist_batch_occupancy(centre_ctx *ctx, int tile, int threads, int nb, int *per_sm);
+int launch_pairs_hist_batch(centre_ctx *ctx, const BatchSys *d_sys, int nsys, uint64_t nitems,
+                            const BatchCommon &B, int tile, int threads, int grid,
+                            const double *d_tab);
 int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uint32_t *d_pairs,
                       int all_pairs, uint32_t ndof, const double *d_ext, const double *d_lsum,
                       const U128 *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
@@ -168,6 +194,10 @@ struct ScoreParams {
   uint32_t type_start[4];
   uint32_t type_count[4];
 };
+size_t score_scratch_bytes(const ScoreParams &S, bool tree);
+int launch_score_async(centre_ctx *ctx, const ScoreParams &S, const uint8_t *d_types,
+                       const uint32_t *d_pairs, const double *d_s1, const double *d_s2,
+                       double *d_mi, double *d_mie, double *d_mist, void *d_scratch);
 int launch_score(centre_ctx *ctx, const ScoreParams &S, const uint8_t *d_types,
                  const uint32_t *d_pairs, const double *d_s1, const double *d_s2, double *d_mi,
                  double *h_mie, int build_tree, double *h_mist, uint32_t *h_tree,

@@ -286,7 +286,127 @@ __global__ void mst_gather_kernel(const __grid_constant__ ScoreParams S,
   ij[2 * idx + 1] = j;
 }
 
+// MIST rows on the device: tree MI summed per type block, S2 = S1 - sum
+// (src/EntropyScorer.cpp:769-799).  One CTA per graph.
+__global__ void mist_sums_kernel(const __grid_constant__ ScoreParams S,
+                                 const uint8_t *__restrict__ types,
+                                 const uint32_t *__restrict__ pairs,
+                                 const double *__restrict__ mi, const uint32_t *__restrict__ tree,
+                                 const uint32_t *__restrict__ ntree, uint32_t cap,
+                                 const double *__restrict__ mie, double *__restrict__ mist) {
+  const int g = blockIdx.x;
+  __shared__ double blk[6][256];
+  double a[6] = {0, 0, 0, 0, 0, 0};
+  const uint32_t nt = min(ntree[g], cap);
+  for (uint32_t e = threadIdx.x; e < nt; e += blockDim.x) {
+    const uint64_t p = tree[(uint64_t)g * (cap + 1) + e];
+    uint32_t i, j;
+    pair_of(S, pairs, p, i, j);
+    const int b = block_of(types[i], types[j]);
+    if (b >= 0) a[b] += mi[p * S.G + g];
+  }
+  for (int q = 0; q < 6; ++q) blk[q][threadIdx.x] = a[q];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double *row = mie + (uint64_t)g * kCols;
+    double *out = mist + (uint64_t)g * kCols;
+    for (int c = 0; c < kCols; ++c) out[c] = row[c];
+    double d = row[15];
+    for (int q = 0; q < 6; ++q) {
+      double sum = 0.0;
+      for (int l = 0; l < (int)blockDim.x; ++l) sum += blk[q][l];
+      out[4 + 2 * q] = sum;
+      d -= sum;
+    }
+    out[16] = d;
+  }
+}
+
 }  // namespace
+
+size_t score_scratch_bytes(const ScoreParams &S, bool tree) {
+  const int G = S.G;
+  const uint64_t chunk = 4096;
+  const uint64_t nchunks = std::max<uint64_t>(1, (S.npairs + chunk - 1) / chunk);
+  size_t b = sizeof(double) * nchunks * G * 12 + 256;
+  if (tree) {
+    const uint64_t GV = (uint64_t)G * S.ndof;
+    const uint64_t cap = S.ndof > 0 ? S.ndof - 1 : 0;
+    b += sizeof(uint32_t) * GV * 2 + sizeof(unsigned long long) * GV * 3 +
+         sizeof(uint32_t) * ((uint64_t)G * (cap + 1) + G + 1) + 256;
+  }
+  return b;
+}
+
+// Everything on the stream, no host synchronisation (capturable): MI, the
+// MIE rows into d_mie, and with d_mist the spanning tree after a fixed
+// number of Boruvka rounds (each round at least halves the component count,
+// so ceil(log2 V) + 1 rounds always finish; extra rounds change nothing) and
+// the MIST rows into d_mist.
+int launch_score_async(centre_ctx *ctx, const ScoreParams &S, const uint8_t *d_types,
+                       const uint32_t *d_pairs, const double *d_s1, const double *d_s2,
+                       double *d_mi, double *d_mie, double *d_mist, void *d_scratch) {
+  const int G = S.G;
+  if (G <= 0 || G > 256)
+    return set_error(ctx, CENTRE_E_UNSUPPORTED, "estimators*schemes*steps must be <= 256");
+  const int k = std::max(1, 256 / G);
+  const int threads = G * k;
+  const uint64_t chunk = 4096;
+  const int nchunks = (int)std::max<uint64_t>(1, (S.npairs + chunk - 1) / chunk);
+  double *d_part = reinterpret_cast<double *>(d_scratch);
+  KernelTimer kt(ctx, CENTRE_TIMER_SCORE);
+  CENTRE_CUDA(ctx, cudaMemsetAsync(d_part, 0, sizeof(double) * (size_t)nchunks * G * 12, ctx->stream));
+  if (S.npairs) {
+    mi_sums_kernel<<<nchunks, threads, sizeof(double) * threads * 12, ctx->stream>>>(
+        S, d_types, d_pairs, d_s1, d_s2, d_mi, d_part, chunk);
+    ctx->launches++;
+  }
+  sums_final_kernel<<<G, 256, 0, ctx->stream>>>(S, d_types, d_s1, d_part, nchunks, d_mie);
+  ctx->launches++;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  if (!d_mist) return CENTRE_OK;
+  unsigned char *base = reinterpret_cast<unsigned char *>(d_scratch) +
+                        ((sizeof(double) * (size_t)nchunks * G * 12 + 255) & ~size_t(255));
+  const uint64_t GV = (uint64_t)G * S.ndof;
+  const uint32_t cap = S.ndof > 0 ? S.ndof - 1 : 0;
+  uint32_t *comp = reinterpret_cast<uint32_t *>(base);
+  uint32_t *parent = comp + GV;
+  unsigned long long *bestkey = reinterpret_cast<unsigned long long *>(parent + GV);
+  unsigned long long *bestedge = bestkey + GV;
+  unsigned long long *winpair = bestedge + GV;
+  uint32_t *tree = reinterpret_cast<uint32_t *>(winpair + GV);
+  uint32_t *ntree = tree + (uint64_t)G * (cap + 1);
+  unsigned *added = ntree + G;
+  const unsigned TB = 256;
+  auto blocks = [&](uint64_t n) { return (unsigned)((n + TB - 1) / TB); };
+  mst_init_kernel<<<blocks(GV), TB, 0, ctx->stream>>>(comp, S.ndof, GV);
+  mst_init_kernel<<<blocks(GV), TB, 0, ctx->stream>>>(parent, S.ndof, GV);
+  ctx->launches += 2;
+  CENTRE_CUDA(ctx, cudaMemsetAsync(ntree, 0, sizeof(uint32_t) * (G + 1), ctx->stream));
+  const uint64_t PG = S.npairs * (uint64_t)G;
+  int rounds = 1;
+  while ((1u << (rounds - 1)) < S.ndof) ++rounds;
+  for (int r = 0; r < rounds && PG > 0; ++r) {
+    mst_reset_kernel<<<blocks(GV), TB, 0, ctx->stream>>>(bestkey, bestedge, GV);
+    mst_pick_kernel<0><<<blocks(PG), TB, 0, ctx->stream>>>(S, d_types, d_pairs, d_mi, comp,
+                                                           bestkey, bestedge);
+    mst_pick_kernel<1><<<blocks(PG), TB, 0, ctx->stream>>>(S, d_types, d_pairs, d_mi, comp,
+                                                           bestkey, bestedge);
+    mst_hook_kernel<<<blocks(PG), TB, 0, ctx->stream>>>(S, d_types, d_pairs, d_mi, comp, parent,
+                                                        bestkey, bestedge, winpair, tree, ntree,
+                                                        cap, added);
+    mst_link_kernel<<<blocks(GV), TB, 0, ctx->stream>>>(S, d_pairs, comp, parent, bestedge,
+                                                        winpair, tree, ntree, cap, added);
+    mst_jump_kernel<<<blocks(GV), TB, 0, ctx->stream>>>(S, comp, parent);
+    mst_parent_sync_kernel<<<blocks(GV), TB, 0, ctx->stream>>>(S, comp, parent);
+    ctx->launches += 7;
+  }
+  mist_sums_kernel<<<G, 256, 0, ctx->stream>>>(S, d_types, d_pairs, d_mi, tree, ntree, cap, d_mie,
+                                               d_mist);
+  ctx->launches++;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  return CENTRE_OK;
+}
 
 int launch_score(centre_ctx *ctx, const ScoreParams &S, const uint8_t *d_types,
                  const uint32_t *d_pairs, const double *d_s1, const double *d_s2, double *d_mi,

@@ -97,3 +97,88 @@ WORKLOADS = {
     "chain1000": dict(natoms=1000, nframes=100_000, nbins=50, nsteps=10, coupling="block8"),
     "chain5000": dict(natoms=5000, nframes=100_000, nbins=50, nsteps=10, coupling="block8"),
 }
+
+# Batched trajectories of uneven size: 16 chains of 200..1200 atoms with
+# 20,000..150,000 frames (sizes and lengths paired by a seeded permutation),
+# 40 bins, 10 convergence steps.
+BATCHES = {
+    "batch16": dict(nsys=16, atoms=(200, 1200), frames=(20_000, 150_000), nbins=40, nsteps=10,
+                    coupling="block8"),
+    "batch4": dict(nsys=4, atoms=(40, 120), frames=(5_000, 30_000), nbins=40, nsteps=10,
+                   coupling="block8"),
+}
+
+
+def batch_specs(name: str, seed: int = 0):
+    """(natoms, nframes, seed) of every trajectory of a named batch."""
+    b = BATCHES[name]
+    n = b["nsys"]
+    atoms = np.linspace(b["atoms"][0], b["atoms"][1], n).round().astype(int)
+    frames = np.linspace(b["frames"][0], b["frames"][1], n).round().astype(int)
+    frames = frames[np.random.default_rng(seed).permutation(n)]
+    return [(int(a), int(f), seed * 1000 + k) for k, (a, f) in enumerate(zip(atoms, frames))]
+
+
+def _vonmises_torch(torch, shape, kappa, gen, device):
+    """Von Mises(0, kappa) samples by the Best-Fisher (1979) rejection method."""
+    tau = 1.0 + np.sqrt(1.0 + 4.0 * kappa * kappa)
+    rho = (tau - np.sqrt(2.0 * tau)) / (2.0 * kappa)
+    r = (1.0 + rho * rho) / (2.0 * rho)
+    out = torch.empty(shape, dtype=torch.float64, device=device).view(-1)
+    todo = torch.arange(out.numel(), device=device)
+    while todo.numel():
+        m = todo.numel()
+        u = torch.rand((3, m), generator=gen, device=device, dtype=torch.float64)
+        z = torch.cos(np.pi * u[0])
+        f = (1.0 + r * z) / (r + z)
+        c = kappa * (r - f)
+        ok = (c * (2.0 - c) - u[1] > 0) | (torch.log(c / u[1]) + 1.0 - c >= 0)
+        th = torch.sign(u[2] - 0.5) * torch.acos(f.clamp(-1.0, 1.0))
+        out[todo[ok]] = th[ok]
+        todo = todo[~ok]
+    return out.view(shape)
+
+
+def chain_blocks_torch(natoms: int, nframes: int, seed: int, device, coupling: str = "block8",
+                       kappa: float = 8.0, p_share: float = 0.7):
+    """The chain of ``chain_trajectory`` (same distributions and coupling)
+    drawn on a device with torch, for workloads too large to generate on
+    the host: [(bat_type, float32 tensor [k][nframes])] for bonds, angles,
+    torsions."""
+    import torch
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    nb, na, nt = natoms - 1, natoms - 2, natoms - 3
+    bonds = (torch.randn((nb, nframes), generator=gen, device=device) * 0.03 + 1.5).float()
+    angles = (torch.randn((na, nframes), generator=gen, device=device) * 0.08 + 1.91)
+    angles = angles.clamp(1e-3, np.pi - 1e-3).float()
+    cum = torch.tensor(np.cumsum(WEIGHTS), device=device)
+    modes_v = torch.tensor(MODES, device=device)
+
+    def draw(size):
+        u = torch.rand(size, generator=gen, device=device, dtype=torch.float64)
+        return torch.searchsorted(cum, u, right=True).clamp(max=len(WEIGHTS) - 1)
+
+    tors = torch.empty((nt, nframes), dtype=torch.float32, device=device)
+    step = 8 if coupling == "block8" else nt
+    prev = None
+    for b0 in range(0, nt, step):
+        b1 = min(nt, b0 + step)
+        k = b1 - b0
+        fresh = draw((k, nframes))
+        keep = torch.rand((k, nframes), generator=gen, device=device) < p_share
+        if coupling == "block8":
+            latent = draw((1, nframes)).expand(k, nframes)
+            modes = torch.where(keep, latent, fresh)
+        else:
+            modes = fresh.clone()
+            for t in range(k):
+                src = prev if t == 0 else modes[t - 1]
+                if src is not None:
+                    modes[t] = torch.where(keep[t], src, fresh[t])
+            prev = modes[-1]
+        ang = modes_v[modes] + _vonmises_torch(torch, (k, nframes), kappa, gen, device)
+        ang = torch.remainder(ang, TWO_PI).float()
+        ang[ang >= np.float32(TWO_PI)] = 0.0
+        tors[b0:b1] = ang
+    return [(1, bonds), (2, angles), (3, tors)]

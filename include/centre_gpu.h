@@ -233,6 +233,40 @@ int centre_gpu_score_dev(centre_ctx *ctx, const centre_entropy_params *p,
                          double *mie_sums, double *mist_sums, uint32_t *tree,
                          uint32_t *ntree);
 
+/* -------------------------------------------------------------- batch ---- */
+/* One trajectory of a batch: device arrays in the single-trajectory layouts
+ * above (types [ndof], bins [ndof][nschemes][nframes], extremes [ndof][4],
+ * s1 [ndof][est][sch][steps], s2 [ndof*(ndof-1)/2][est][sch][steps] over all
+ * pairs i<j, mi like s2 or NULL) and host rows for the sums
+ * (mie_sums, mist_sums [est][sch][steps][CENTRE_SUMS_COLS]; mist_sums may be
+ * NULL to skip the spanning tree).  Each trajectory has its own frame count;
+ * the convergence steps are prefixes of it (src/Estimators.cpp:162-188). */
+typedef struct centre_system {
+  uint32_t ndof;
+  uint64_t nframes;
+  const uint8_t *types;
+  const uint8_t *bins;
+  const double *extremes;
+  double *s1;
+  double *s2;
+  double *mi;
+  double *mie_sums;
+  double *mist_sums;
+} centre_system;
+
+/* EntropyCalculator::run (src/EntropyCalculator.cpp:1090) followed by
+ * EntropyScorer::run (src/EntropyScorer.cpp:7) for nsys trajectories at
+ * once: 1-D entropies, all-pairs joint entropies (one persistent count
+ * kernel over every trajectory's pair tiles), MI, MIE sums and, where asked,
+ * the MIST tree sums.  The work is captured into one CUDA graph, cached by
+ * the call's arguments and replayed when the same batch comes back; the
+ * count kernel's tile shape and block size are tuned on the first call for
+ * each (bins, steps, schemes).  ML and MM estimators; p->nframes is ignored
+ * (each trajectory's nframes is used).  Returns after the sums are on the
+ * host. */
+int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entropy_params *p,
+                                 uint32_t nsys, const centre_system *sys);
+
 #ifdef __cplusplus
 }
 #endif
