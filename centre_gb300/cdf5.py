@@ -353,3 +353,35 @@ def write_bins(path: str, content: str, dimid, extremes, coord, bin_schemes):
         "coord": Variable("coord", ("dims", "bin_scheme_count", "frames"), 7, {}, coord),
     }
     write(path, ds)
+
+
+# ------------------------------------------------------- BAT trajectories --
+def write_bat(path: str, bonds, angles, torsions, time=None, version: int = 5):
+    """A CENTRE BAT trajectory as Netcdf_BAT reads it (src/Netcdf_BAT.cpp:
+    24-132, 236-330): global attribute convention = "CENTRE", record
+    dimension "frame", variables time [frame], bond [frame][bond], angle
+    [frame][angle], dihedral [frame][dihedral] (float32).  Inputs are
+    DOF-major [ndof][nframes] arrays."""
+    b = np.ascontiguousarray(np.asarray(bonds, np.float32).T)
+    a = np.ascontiguousarray(np.asarray(angles, np.float32).T)
+    d = np.ascontiguousarray(np.asarray(torsions, np.float32).T)
+    nfr = b.shape[0]
+    t = np.arange(nfr, dtype=np.float32) if time is None else np.asarray(time, np.float32)
+    ds = Dataset(version=version)
+    ds.dims = {"frame": 0, "bond": b.shape[1], "angle": a.shape[1], "dihedral": d.shape[1]}
+    ds.attrs = {"title": "BAT trajectory", "application": "CENTRE", "program": "centre_gb300",
+                "programVersion": "1.0.0", "convention": "CENTRE", "conventionVersion": "1.0",
+                "hasPseudo": "N"}
+    ds.vars = {
+        "time": Variable("time", ("frame",), 5, {"units": "picosecond"}, t),
+        "bond": Variable("bond", ("frame", "bond"), 5, {"units": "angstrom"}, b),
+        "angle": Variable("angle", ("frame", "angle"), 5, {"units": "radian"}, a),
+        "dihedral": Variable("dihedral", ("frame", "dihedral"), 5, {"units": "radian"}, d),
+    }
+    write(path, ds)
+
+
+def read_entcontri(path: str):
+    """entcontri_*.nc -> (ids [records][order] uint32, contri_S [records][est][sch][steps])."""
+    ds = read(path)
+    return ds.vars["id"].data.astype(np.uint32), ds.vars["contri_S"].data.astype(np.float64)
