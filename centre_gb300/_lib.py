@@ -42,6 +42,32 @@ class System(C.Structure):
     ]
 
 
+class ScreenParams(C.Structure):
+    """centre_screen_params: learned pair screen."""
+    _fields_ = [
+        ("feat_div", C.c_uint32),
+        ("ntrain", C.c_uint32),
+        ("nprefilter", C.c_uint32),
+        ("nneigh", C.c_uint32),
+        ("epochs", C.c_uint32),
+        ("batch", C.c_uint32),
+        ("lr", C.c_float),
+        ("train", C.c_uint8),
+        ("init_weights", C.c_uint8),
+        ("seed", C.c_uint64),
+    ]
+
+
+SCREEN_NPARAMS = 5057
+
+
+def make_screen_params(feat_div=5, ntrain=200_000, nprefilter=256, nneigh=64, epochs=3,
+                       batch=4096, lr=2e-3, train=True, init_weights=True, seed=1):
+    return ScreenParams(int(feat_div), int(ntrain), int(nprefilter), int(nneigh), int(epochs),
+                        int(batch), float(lr), 1 if train else 0, 1 if init_weights else 0,
+                        int(seed))
+
+
 class EntropyParams(C.Structure):
     _fields_ = [
         ("nframes", C.c_uint64),
@@ -111,6 +137,11 @@ _SIGS = {
                                        C.c_uint64, _vp, _vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     "centre_gpu_entropy_batch_dev": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32,
                                                C.POINTER(System)]),
+    "centre_gpu_screen_dev": (C.c_int, [_vp, C.POINTER(EntropyParams), C.POINTER(ScreenParams),
+                                        C.c_uint32, _vp, _vp, _vp, _vp, _vp, C.c_uint64, _vp,
+                                        C.POINTER(C.c_uint64)]),
+    "centre_gpu_screen_mlp_grad": (C.c_int, [_vp, _vp, C.c_uint64, _vp, _vp, _vp, _vp,
+                                             C.POINTER(C.c_double)]),
 }
 
 _lib = None

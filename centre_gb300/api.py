@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import CentreError, EntropyParams, make_params, SUMS_COLS, SUMS_NAMES  # noqa: F401
-from ._lib import System
+from ._lib import System, ScreenParams, make_screen_params, SCREEN_NPARAMS  # noqa: F401
 
 BOND, ANGLE, DIHEDRAL = 1, 2, 3
 ML, MM, CS, JS = 0, 1, 2, 3
@@ -261,3 +261,34 @@ class Context:
         self.check(self.L.centre_gpu_entropy_batch_dev(self.h, C.byref(params), len(systems),
                                                        arr))
         return [{"mie": m, "mist": t} for m, t in keep]
+
+    # ---------------------------------------------------------- pair screen --
+    def screen_dev(self, params, sparams, types, bins, ext, weights=None):
+        """Learned neighbour selection (centre_gpu_screen_dev) on CUDA tensors.
+        Returns (pairs: CUDA uint32-as-int32 tensor [npairs][2], weights
+        float32 [SCREEN_NPARAMS], losses float32 [epochs])."""
+        import torch
+        ndof = int(bins.shape[0])
+        w = (np.zeros(SCREEN_NPARAMS, np.float32) if weights is None
+             else np.ascontiguousarray(weights, np.float32).copy())
+        losses = np.zeros(max(int(sparams.epochs), 1), np.float32)
+        cap = ndof * int(sparams.nneigh)
+        pairs = torch.empty((cap, 2), dtype=torch.int32, device=bins.device)
+        n = C.c_uint64(0)
+        self.check(self.L.centre_gpu_screen_dev(self.h, C.byref(params), C.byref(sparams), ndof,
+                                                _ptr(types), _ptr(bins), _ptr(ext), _ptr(w),
+                                                _ptr(losses), cap, _ptr(pairs), C.byref(n)))
+        return pairs[: n.value], w, losses[: int(sparams.epochs)]
+
+    def screen_mlp_grad(self, weights, feats, targets):
+        """One forward/backward pass of the screen network: (pred, grad, loss)."""
+        w = np.ascontiguousarray(weights, np.float32)
+        x = np.ascontiguousarray(feats, np.float32)
+        y = np.ascontiguousarray(targets, np.float32)
+        n = len(y)
+        pred = np.empty(n, np.float32)
+        grad = np.empty(SCREEN_NPARAMS, np.float32)
+        loss = C.c_double(0)
+        self.check(self.L.centre_gpu_screen_mlp_grad(self.h, _ptr(w), n, _ptr(x), _ptr(y),
+                                                     _ptr(pred), _ptr(grad), C.byref(loss)))
+        return pred, grad, loss.value

@@ -418,6 +418,7 @@ void centre_gpu_destroy(centre_ctx *ctx) {
   }
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
   centre::batch_state_free(ctx);
+  centre::screen_state_free(ctx);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

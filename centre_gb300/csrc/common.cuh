@@ -52,6 +52,7 @@ struct centre_ctx {
   double timer_ms[4] = {0, 0, 0, 0};
   uint64_t timer_n[4] = {0, 0, 0, 0};
   void *batch_state = nullptr;  // tuned tiles and the cached batch graph
+  void *cublas = nullptr;       // cuBLAS handle of the pair screen's correlation GEMM
 };
 
 namespace centre {
@@ -73,6 +74,7 @@ int check_cuda(centre_ctx *ctx, cudaError_t e, const char *what);
 void *scratch(centre_ctx *ctx, int slot, size_t bytes, int *status);
 void *ctx_clnc(centre_ctx *ctx);
 void batch_state_free(centre_ctx *ctx);
+void screen_state_free(centre_ctx *ctx);
 
 // Scoped event timer around a launch on the context's stream (no-op unless
 // timing is enabled).

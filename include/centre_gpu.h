@@ -267,6 +267,50 @@ typedef struct centre_system {
 int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entropy_params *p,
                                  uint32_t nsys, const centre_system *sys);
 
+/* -------------------------------------------------------- pair screen ---- */
+/* Learned neighbour selection for A-MIE / A-MIST.  The reference takes the
+ * pairs of its approximate methods from a neighbour file made outside the
+ * program (useneighbor=true, Neighbors(fname), src/Centre.cpp:459-593);
+ * this selects them from the data.  A BF16 MLP 12 -> 64 -> 64 -> 1 scores
+ * the partners that pass a correlation prefilter from 12 per-pair features
+ * (prefix marginal entropies, DOF types, index distance within the type,
+ * the 2x2 correlation block of (cos, sin) or standardised bin columns, a
+ * Gaussian MI proxy); the network is trained on exact MI of random pairs at
+ * the first of feat_div convergence steps.  No reference counterpart. */
+#define CENTRE_SCREEN_NPARAMS 5057
+typedef struct centre_screen_params {
+  uint32_t feat_div;    /* features and labels use the first nframes/feat_div frames */
+  uint32_t ntrain;      /* random training pairs                                 */
+  uint32_t nprefilter;  /* partners per DOF kept by the correlation prefilter   */
+  uint32_t nneigh;      /* partners per DOF kept by the network                 */
+  uint32_t epochs;      /* training epochs                                       */
+  uint32_t batch;       /* minibatch size                                        */
+  float lr;             /* Adam learning rate                                    */
+  uint8_t train;        /* 1: train the network here, 0: use weights as given   */
+  uint8_t init_weights; /* with train: start from seeded random weights         */
+  uint64_t seed;
+} centre_screen_params;
+
+/* Device inputs as centre_gpu_entropy1d_dev (DOF types in bonds, angles,
+ * torsions order); weights [CENTRE_SCREEN_NPARAMS] host FP32 (in, and the
+ * trained weights out when training), losses [epochs] host mean squared
+ * error per epoch (may be NULL); pairs: device [capacity][2] out, every
+ * selected pair i<j in row-major order, *npairs their number (capacity
+ * ndof*nneigh always suffices). */
+int centre_gpu_screen_dev(centre_ctx *ctx, const centre_entropy_params *p,
+                          const centre_screen_params *sp, uint32_t ndof,
+                          const uint8_t *types, const uint8_t *bins,
+                          const double *extremes, float *weights, float *losses,
+                          uint64_t capacity, uint32_t *pairs, uint64_t *npairs);
+
+/* One forward and backward pass of the screen network over n samples
+ * (host arrays): feats [n][12], targets [n]; pred [n] (may be NULL), grad
+ * [CENTRE_SCREEN_NPARAMS] of the mean squared error, *loss that error.
+ * Exposes the training kernels for gradient checks. */
+int centre_gpu_screen_mlp_grad(centre_ctx *ctx, const float *weights, uint64_t n,
+                               const float *feats, const float *targets, float *pred,
+                               float *grad, double *loss);
+
 #ifdef __cplusplus
 }
 #endif
