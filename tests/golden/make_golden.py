@@ -17,6 +17,12 @@ stores inputs and outputs:
   vmkde_ref.npz       Real2Int::getMinimaPositions (src/Real2Int.cpp:481-716)
   example1.npz/.json  the bin files and expected CSV values shipped in the
                       reference's test_examples/example-1/outfiles-h-ref
+  example1_entcontri.npz  the DOF/pair ids and contri_S entropies of that
+                      example's entcontri_*.nc files (HDF5, read with
+                      hdf5_min.py): the reference's own 1-D and 2-D entropies
+                      of the subset DOFs and neighbour pairs
+
+    python tests/golden/make_golden.py example1     # only the example-1 fixtures
 """
 from __future__ import annotations
 
@@ -155,6 +161,9 @@ def make_example1():
     head = [h.strip() for h in rows[0]]
     meta["mie_columns"] = head
     meta["mie_rows"] = [[float(x) for x in r] for r in rows[1:] if r]
+    with open(os.path.join(base, "MIST-ML_convergence_b-30.csv")) as f:
+        rows = list(csv.reader(f))
+    meta["mist_rows"] = [[float(x) for x in r] for r in rows[1:] if r]
     trees = {}
     for s in range(4):
         with open(os.path.join(base, f"Tree-MIST-ML_b-30_s-{s}.csv")) as f:
@@ -167,9 +176,20 @@ def make_example1():
     np.savez_compressed(os.path.join(HERE, "example1.npz"), **out)
     with open(os.path.join(HERE, "example1.json"), "w") as f:
         json.dump(meta, f, indent=1)
+    sys.path.insert(0, HERE)
+    import hdf5_min
+    ent = {}
+    for f in ("bnd-1d", "ang-1d", "tor-1d", "bnd-2d", "ang-2d", "tor-2d", "ba-2d", "bd-2d", "ad-2d"):
+        ids, contri = hdf5_min.read_entcontri(os.path.join(base, f"entcontri_{f}.nc"))
+        key = f.replace("-", "_")
+        ent[f"{key}_ids"], ent[f"{key}_contri"] = ids, contri
+    np.savez_compressed(os.path.join(HERE, "example1_entcontri.npz"), **ent)
 
 
 if __name__ == "__main__":
+    if sys.argv[1:] == ["example1"]:
+        make_example1()
+        sys.exit(0)
     oracle.build(with_ref=True)
     R = oracle.Reference()
     disc = make_discretize(R)

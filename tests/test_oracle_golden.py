@@ -101,3 +101,84 @@ def test_example1_tree_edge_mi(orc, ex1):
         mi = s1[pairs[:, 0], 0, 0, step] + s1[pairs[:, 1], 0, 0, step] - s2[:, 0, 0, step]
         want = np.array([e[4] for e in edges])
         assert np.max(np.abs(mi - want)) <= 0.5e-6 + 1e-9
+
+
+# ---- the reference's own entropy-contribution files of example 1 ---------
+BLOCKS2D = (("bnd_2d", "B", "B"), ("ba_2d", "B", "A"), ("bd_2d", "B", "T"),
+            ("ang_2d", "A", "A"), ("ad_2d", "A", "T"), ("tor_2d", "T", "T"))
+
+
+@pytest.fixture(scope="module")
+def ex1ent():
+    return np.load(os.path.join(GOLDEN, "example1_entcontri.npz"))
+
+
+def _ex1_arrays(d):
+    names = {"B": "bonds", "A": "angles", "T": "torsions"}
+    tcode = {"B": 1, "A": 2, "T": 3}
+    coord = np.concatenate([d[f"{names[k]}_coord"] for k in "BAT"])
+    ext = np.concatenate([d[f"{names[k]}_ext"] for k in "BAT"])
+    types = np.concatenate([np.full(len(d[f"{names[k]}_coord"]), tcode[k], np.uint8) for k in "BAT"])
+    off = {"B": 0, "A": len(d["bonds_coord"]), "T": len(d["bonds_coord"]) + len(d["angles_coord"])}
+    return coord, ext, types, off
+
+
+def test_example1_entcontri_matches_oracle(orc, ex1, ex1ent):
+    """The oracle's 1-D and 2-D entropies of the example's subset DOFs and
+    neighbour pairs against the values the reference wrote to its
+    entcontri_*.nc files (ML, 30 bins, 4 steps, Jacobian on)."""
+    d, _ = ex1
+    coord, ext, types, off = _ex1_arrays(d)
+    s1 = orc.entropy1d(types, coord, ext, 4, [30], [0], True)
+    for f, k in (("bnd_1d", "B"), ("ang_1d", "A"), ("tor_1d", "T")):
+        ids = ex1ent[f + "_ids"][:, 0].astype(np.int64)
+        np.testing.assert_allclose(s1[off[k] + ids], ex1ent[f + "_contri"], rtol=1e-9, atol=1e-13)
+    for f, a, b in BLOCKS2D:
+        ids = ex1ent[f + "_ids"].astype(np.int64)
+        pairs = np.stack([off[a] + ids[:, 0], off[b] + ids[:, 1]], 1).astype(np.uint32)
+        s2 = orc.entropy2d(pairs, types, coord, ext, 4, [30], [0], True)
+        np.testing.assert_allclose(s2, ex1ent[f + "_contri"], rtol=1e-9, atol=1e-13)
+
+
+def test_example1_sums_and_tree_from_reference_entropies(orc, ex1, ex1ent):
+    """MIE and MIST rows of the shipped CSVs, and every shipped tree, rebuilt
+    from the reference's own entropies: the block sums, MI and the spanning
+    tree over the neighbour pairs in the reference's edge order (B/B, B/A,
+    B/D, A/A, A/D, D/D)."""
+    _, meta = ex1
+    s1 = {k: ex1ent[f + "_contri"][:, 0, 0, :] for f, k in (("bnd_1d", "B"), ("ang_1d", "A"),
+                                                            ("tor_1d", "T"))}
+    id2idx = {k: {int(i): n for n, i in enumerate(ex1ent[f + "_ids"][:, 0])}
+              for f, k in (("bnd_1d", "B"), ("ang_1d", "A"), ("tor_1d", "T"))}
+    base = {"B": 0, "A": len(s1["B"]), "T": len(s1["B"]) + len(s1["A"])}
+    cols = meta["mie_columns"]
+    for step in range(4):
+        mie = meta["mie_rows"][step]
+        mist = meta["mist_rows"][step]
+        for k, c in (("B", "BOND-S1"), ("A", "ANGLE-S1"), ("T", "DIHED-S1")):
+            assert abs(s1[k][:, step].sum() - mie[cols.index(c)]) <= 0.5e-4 + 1e-9
+        src, dst, w, tag = [], [], [], []
+        for f, a, b in BLOCKS2D:
+            ids = ex1ent[f + "_ids"]
+            s2 = ex1ent[f + "_contri"][:, 0, 0, step]
+            ia = np.array([id2idx[a][int(x)] for x in ids[:, 0]])
+            ib = np.array([id2idx[b][int(x)] for x in ids[:, 1]])
+            mi = s1[a][ia, step] + s1[b][ib, step] - s2
+            name = {"B": "B", "A": "A", "T": "D"}
+            c = f"{name[a]}/{name[b]}"
+            assert abs(s2.sum() - mie[cols.index(c + "-S2")]) <= 0.5e-4 + 1e-9
+            assert abs(mi.sum() - mie[cols.index(c + "-I2")]) <= 0.5e-4 + 1e-9
+            src += list(base[a] + ia)
+            dst += list(base[b] + ib)
+            w += list(mi)
+            tag += [c] * len(mi)
+        tree = orc.mst(base["T"] + len(s1["T"]), src, dst, w)
+        tot = {c: 0.0 for c in set(tag)}
+        for e in tree:
+            tot[tag[e]] += w[e]
+        for c, v in tot.items():
+            assert abs(v - mist[cols.index(c + "-I2")]) <= 0.5e-4 + 1e-9, (step, c)
+        inv = {v: (k, i) for k in "BAT" for i, v in ((i, base[k] + n) for i, n in id2idx[k].items())}
+        got = sorted((inv[src[e]][0], inv[dst[e]][0], inv[src[e]][1], inv[dst[e]][1]) for e in tree)
+        want = sorted((a, b, i, j) for a, b, i, j, _ in meta["trees"][str(step)])
+        assert got == want, step
