@@ -123,9 +123,12 @@ def cpu_sample_rate(tr, target_s=8.0, nthreads=None, seed=0):
     # discretise a DOF sample of each type
     t0 = time.perf_counter()
     nd = 0
-    bins_l, ext_l, types_l = [], [], []
+    bins_l, ext_l, types_l, glob = [], [], [], []
+    base = 0
     for typ, blk in blocks:
         k = min(len(blk), 24)
+        glob += list(range(base, base + k))
+        base += len(blk)
         b, e = orc.discretize(typ, blk[:k], [NBINS], nthreads=nthreads)
         bins_l.append(b)
         ext_l.append(e)
@@ -148,14 +151,16 @@ def cpu_sample_rate(tr, target_s=8.0, nthreads=None, seed=0):
         pairs = rng.integers(0, n, size=(npair, 2)).astype(np.uint32)
         pairs = pairs[pairs[:, 0] != pairs[:, 1]]
         t0 = time.perf_counter()
-        orc.entropy2d(pairs, types, bins, ext, NSTEPS, [NBINS], [0], True, nthreads=nthreads)
+        s2 = orc.entropy2d(pairs, types, bins, ext, NSTEPS, [NBINS], [0], True, nthreads=nthreads)
         dt = time.perf_counter() - t0
         spent += dt
         t_pair = dt / len(pairs)
         if dt > target_s / 4 or spent > target_s:
             break
         npair = int(npair * min(8.0, max(2.0, (target_s / 3) / max(dt, 1e-3))))
-    return t_disc, t_1d, t_pair, len(pairs), nthreads
+    g = np.array(glob, np.int64)
+    check = (np.stack([g[pairs[:, 0]], g[pairs[:, 1]]], 1), s2[:, 0, 0, :])
+    return t_disc, t_1d, t_pair, len(pairs), nthreads, check
 
 
 def cpu_pairs_per_s(w, t_disc, t_1d, t_pair):
@@ -297,13 +302,20 @@ def run_ours(args):
     if not args.no_e2e:
         out["e2e"] = run_e2e(ctx, tr, args, w, world, dist, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        t_d, t_1, t_p, ns, cores = cpu_sample_rate(tr, target_s=args.cpu_seconds)
+        t_d, t_1, t_p, ns, cores, (gp, s2o) = cpu_sample_rate(tr, target_s=args.cpu_seconds)
+        # the GPU's joint entropies of the same pairs against the oracle's
+        i, j = np.minimum(gp[:, 0], gp[:, 1]), np.maximum(gp[:, 0], gp[:, 1])
+        idx = i * ndof - i * (i + 1) // 2 + (j - i - 1)
+        s2g = s2.reshape(npairs, NSTEPS)[torch.from_numpy(idx).to(dev)].cpu().numpy()
+        rel = np.abs(s2g - s2o) / np.maximum(np.abs(s2o), 1e-13)
         out["cpu_baseline"] = {
             "value": cpu_pairs_per_s(w, t_d, t_1, t_p), "unit": UNIT, "cores": cores,
             "kind": "port",
             "sample": f"{ns} random DOF pairs x {n} frames (count+entropy) and 72 DOFs "
                       f"discretised on {cores} host threads, extrapolated to {npairs} pairs; "
-                      "MST excluded"}
+                      "MST excluded",
+            "gpu_vs_oracle_s2": {"pairs": int(len(idx)) * NSTEPS,
+                                 "max_rel_error": float(rel.max())}}
     ctx.close()
     if rank == 0:
         print(json.dumps(out))
@@ -503,6 +515,88 @@ def run_batch(args):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------- von Mises KDE path ----
+def run_kde(args):
+    """The KDE discretisation path on the 1000-atom chain: the reference's
+    von Mises KDE conformer binning (Real2Int::getMinimaPositions; kappa 1,
+    up to 5 conformers, 361-point grid) of its 997 torsions over 100,000
+    frames, then KDE entropies (bin width 1), all 496,506 torsion pairs and
+    MIE/MIST, as the reference runs pdfmethod = vonMisesKDE (torsions only).
+    The BAT torsions come from host memory each step (the KDE entry takes
+    host buffers), so the step includes their upload."""
+    import torch
+    from centre_gb300.api import Context, make_params
+    from centre_gb300.synth import chain_blocks_torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    natoms, nframes, nsteps, nconf = 1000, 100_000, 10, 5
+    ctx = Context(local)
+    tors = chain_blocks_torch(natoms, nframes, 2000, dev, coupling="block8")[2][1]
+    h_tors = tors.cpu().numpy()
+    del tors
+    ndof = h_tors.shape[0]
+    npairs = ndof * (ndof - 1) // 2
+    types = torch.full((ndof,), 3, dtype=torch.uint8, device=dev)
+    ext = torch.full((ndof, 4), 1000.0, dtype=torch.float64, device=dev)
+    p = make_params(nframes, nsteps, [nconf], [0], True, kde=True)
+    s1 = torch.empty((ndof, nsteps), dtype=torch.float64, device=dev)
+    s2 = torch.empty((npairs, nsteps), dtype=torch.float64, device=dev)
+    mi = torch.empty_like(s2)
+    times = {"kde": 0.0, "entropy": 0.0, "score": 0.0}
+
+    def step():
+        t0 = time.perf_counter()
+        b, minima, nfound = ctx.discretize_vmkde(h_tors, nconf, 1.0, 5, 1e-4, 1000)
+        bins = torch.from_numpy(b).to(dev)
+        torch.cuda.synchronize(dev)
+        t1 = time.perf_counter()
+        ctx.entropy1d_dev(p, types, bins, ext, s1)
+        ctx.entropy2d_dev(p, types, bins, ext, s2)
+        torch.cuda.synchronize(dev)
+        t2 = time.perf_counter()
+        out = ctx.score_dev(p, types, s1, s2, None, True, mi)
+        t3 = time.perf_counter()
+        times["kde"] += t1 - t0
+        times["entropy"] += t2 - t1
+        times["score"] += t3 - t2
+        return out
+
+    for _ in range(args.warmup):
+        step()
+    for k in times:
+        times[k] = 0.0
+    torch.cuda.synchronize(dev)
+    launches0 = ctx.launches
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+    step_ms = wall * 1e3 / args.steps
+    # grid work: 361 kernel terms per frame per torsion (FP64 exp each)
+    terms = 361.0 * nframes * ndof
+    out = {
+        "metric": METRIC, "value": npairs / (step_ms / 1e3), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded BAT chain, float32 torsions in host memory)",
+        "config": {"workload": f"kde1000: {ndof} torsions, {nframes} frames, von Mises KDE "
+                               f"(kappa 1, <= {nconf} conformers, 361-point grid), {nsteps} "
+                               f"steps, ML, all {npairs} pairs, MIE-2 + MIST",
+                   "l2": "inputs (0.4 GB) larger than L2", "parallelism": "replicas x1"},
+        "stage_ms_per_step": {k: v * 1e3 / args.steps for k, v in times.items()},
+        "kde_terms_per_s": terms / times["kde"] * args.steps,
+        "gpu_launches": ctx.launches - launches0,
+    }
+    clocks = clk.summary()
+    if clocks:
+        out["clocks"] = clocks
+    ctx.close()
+    print(json.dumps(out))
+
+
 # ------------------------------------------------ learned pair screen ----
 def run_screen(args):
     """A-MIST with the learned pair screen (centre_gpu_screen_dev) on the
@@ -623,7 +717,7 @@ def run_reference(args):
     vals = []
     info = None
     for k in range(args.warmup + args.steps):
-        t_d, t_1, t_p, ns, cores = cpu_sample_rate(tr, target_s=args.cpu_seconds, seed=k)
+        t_d, t_1, t_p, ns, cores, _ = cpu_sample_rate(tr, target_s=args.cpu_seconds, seed=k)
         if k >= args.warmup:
             vals.append(cpu_pairs_per_s(w, t_d, t_1, t_p))
             info = (ns, cores)
@@ -663,6 +757,13 @@ def main():
     args = ap.parse_args()
     global NBINS, NSTEPS
     from centre_gb300.synth import BATCHES
+    if args.workload == "kde1000":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the KDE path is measured "
+                              "against the histogram reference arm only"}))
+            return
+        run_kde(args)
+        return
     if args.workload == "screen5000":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the learned screen has no "

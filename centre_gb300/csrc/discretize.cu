@@ -71,11 +71,15 @@ struct Partial {
 
 // --- exact reference arithmetic (double, no contraction) -------------------
 
-// Value the reference bins for input x: x, or fmod(x + c, 2pi).
+// Value the reference bins for input x: x, or fmod(x + c, 2pi).  With x in
+// [0, 2pi) (checked) and c in (0, 2pi], a = RN(x + c) lies in [0, 4pi), and
+// fmod(a, 2pi) is a when a < 2pi and exactly a - 2pi otherwise (fmod is
+// exact, and so is the subtraction by Sterbenz's lemma since 2pi <= a <
+// 2 * 2pi), so the conditional subtraction returns the same double.
 __device__ __forceinline__ double shifted(float x, int dpind, double c) {
   if (dpind == 0) return (double)x;
   double a = __dadd_rn((double)x, c);
-  return fmod(a, kTwoPi);
+  return a >= kTwoPi ? __dsub_rn(a, kTwoPi) : a;
 }
 
 // floor((v - lo) / w) as the reference computes it, before the (t == nb)
@@ -195,7 +199,12 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
   __shared__ DofState st;
 
   const int tid = threadIdx.x;
+  // fit thresholds in shared memory: the lanes of a warp index them by
+  // their own coarse bin, which would serialise on the constant bank
+  __shared__ float tfit_s[kMaxFit + 1];
   for (int i = tid; i < kMaxFit; i += blockDim.x) part[0].hist[i] = 0;
+  if (P.type == 3 && P.optimize)
+    for (int i = tid; i <= P.nfit; i += blockDim.x) tfit_s[i] = P.tfit[i];
   __syncthreads();
 
   // ---- pass 1: stage, min/max/sum, pi-shift sides, coarse occupancy ------
@@ -227,8 +236,8 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
         // evaluated with the reference expression); guess then correct
         int k = (int)(x * (float)(1.0 / P.fit_bs));
         k = min(max(k, 0), P.nfit - 1);
-        while (k > 0 && x < P.tfit[k]) --k;
-        while (k < P.nfit - 1 && x >= P.tfit[k + 1]) ++k;
+        while (k > 0 && x < tfit_s[k]) --k;
+        while (k < P.nfit - 1 && x >= tfit_s[k + 1]) ++k;
         atomicAdd(&part[0].hist[k], 1u);
       }
     }
