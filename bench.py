@@ -35,6 +35,12 @@ NBINS = 50      # set from the workload in main()
 NSTEPS = 10
 
 
+# DRAM bytes per pair of one all-pairs count launch (100,000 frames, 50 bins,
+# 10 steps), from an ncu capture of 176,121 pairs: 61.6 MB read + 14.3 MB
+# written.
+PAIR_TRAFFIC_PER_PAIR = 76.0e6 / 176121
+
+
 def workload(name):
     from centre_gb300.synth import WORKLOADS
     w = dict(WORKLOADS[name])
@@ -276,7 +282,11 @@ def run_ours(args):
                                "score_mst": t_score / args.steps},
         "roofline": {"bound": "tensor", "kernel": "pair counts", "achieved": achieved,
                      "peak": fp8_peak, "unit": "TFLOP/s", "frac": achieved / fp8_peak,
-                     "traffic": None,
+                     "traffic": PAIR_TRAFFIC_PER_PAIR * npairs,
+                     "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu "
+                                     "capture of the same kernel on the 594-DOF chain (100,000 "
+                                     "frames, 50 bins, 10 steps): 76.0 MB for 176,121 pairs, "
+                                     "scaled by pairs to this launch",
                      "note": f"2*N*B^2 flops per pair (B={NBINS} real bins); fp8 peak = 2 x "
                              f"{src} bf16 {bf16:.0f} TF/s"},
         "discretize_roofline": {"bound": "hbm", "achieved": disc_bytes / (disc_ms / 1e3) / 1e9,
@@ -600,7 +610,8 @@ def run_kde(args):
 # ------------------------------------------------ learned pair screen ----
 def run_screen(args):
     """A-MIST with the learned pair screen (centre_gpu_screen_dev) on the
-    5000-atom chain (14,994 DOFs, 100,000 frames, 50 bins, 10 steps): each
+    5000-atom chain (14,994 DOFs; screen1000: the 1000-atom chain), 100,000
+    frames, 50 bins, 10 steps: each
     step trains the network on exact MI of 200,000 random pairs over the
     first 20 % of frames, keeps 64 partners per DOF, computes their exact
     joint entropies over all frames and runs MIE sums and MIST.  The plain
@@ -613,7 +624,8 @@ def run_screen(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    natoms, nframes, nb, nsteps = 5000, 100_000, 50, 10
+    natoms = 1000 if args.workload == "screen1000" else 5000
+    nframes, nb, nsteps = 100_000, 50, 10
     ctx = Context(local)
     stream = torch.cuda.Stream(device=dev)
     ctx.set_stream(stream.cuda_stream)
@@ -684,7 +696,7 @@ def run_screen(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic (seeded BAT chain drawn on the device, float32)",
-        "config": {"workload": f"screen5000: {ndof} DOFs, {nframes} frames, {nb} bins, "
+        "config": {"workload": f"{args.workload}: {ndof} DOFs, {nframes} frames, {nb} bins, "
                                f"{nsteps} steps, ML, A-MIST over the learned screen's pairs "
                                "(value = all-pairs count / step time)",
                    "screen": "train 200000 pairs on first 20% frames, 3 epochs, prefilter 256, "
@@ -754,6 +766,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare-atomic", dest="compare_atomic", action="store_false")
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--nbins", type=int, default=0,
+                    help="override the workload's bin count (bin-count sweeps)")
     args = ap.parse_args()
     global NBINS, NSTEPS
     from centre_gb300.synth import BATCHES
@@ -764,7 +778,7 @@ def main():
             return
         run_kde(args)
         return
-    if args.workload == "screen5000":
+    if args.workload in ("screen5000", "screen1000"):
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the learned screen has no "
                               "reference counterpart (the reference reads neighbour files)"}))
@@ -780,6 +794,8 @@ def main():
         return
     w = workload(args.workload)
     NBINS, NSTEPS = w["nbins"], w["nsteps"]
+    if args.nbins:
+        NBINS = args.nbins
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -108,15 +108,18 @@ __device__ float bisect_first(float a, float b, Pred pred) {
   return __int_as_float(hi);
 }
 
-// Bracketed variant: tries [guess - span, guess + span] first.
+// Bracketed variant: tries [guess - 4, guess + 4] (floats) first, then
+// [guess - 256, guess + 256], then the whole range.  The guess from the
+// double expression is usually within a few floats of the threshold.
 template <class Pred>
 __device__ float bisect_guess(float a, float b, float guess, Pred pred) {
-  const int span = 256;
   int ga = __float_as_int(a), gb = __float_as_int(b);
   int g = __float_as_int(fminf(fmaxf(guess, a), b));
-  int l = max(ga, g - span), h = min(gb, g + span);
-  float fl = __int_as_float(l), fh = __int_as_float(h);
-  if (pred(fh) && (l == ga || !pred(fl))) return bisect_first(fl, fh, pred);
+  for (int span = 4; span <= 256; span *= 64) {
+    int l = max(ga, g - span), h = min(gb, g + span);
+    float fl = __int_as_float(l), fh = __int_as_float(h);
+    if (pred(fh) && (l == ga || !pred(fl))) return bisect_first(fl, fh, pred);
+  }
   return bisect_first(a, b, pred);
 }
 
@@ -247,7 +250,21 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
     const float4 *g4 = reinterpret_cast<const float4 *>(gsrc);
     float4 *s4 = reinterpret_cast<float4 *>(stage);
     uint64_t n4 = cnt >> 2;
-    for (uint64_t i = tid; i < n4; i += blockDim.x) {
+    // four independent 16-byte loads in flight per thread before any use:
+    // the slice streams at HBM rate instead of one load latency per step
+    const uint64_t T = blockDim.x;
+    uint64_t i = tid;
+    for (; i + 3 * T < n4; i += 4 * T) {
+      float4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = __ldg(g4 + i + u * T);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (P.staged) s4[i + u * T] = v[u];
+        visit(v[u].x); visit(v[u].y); visit(v[u].z); visit(v[u].w);
+      }
+    }
+    for (; i < n4; i += T) {
       float4 v = __ldg(g4 + i);
       if (P.staged) s4[i] = v;
       visit(v.x); visit(v.y); visit(v.z); visit(v.w);
