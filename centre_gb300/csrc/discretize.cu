@@ -43,6 +43,7 @@ constexpr int kThreads = 512;
 constexpr int kMaxFit = 180;                   // src/Real2Int.cpp:269
 constexpr int kMaxCluster = 8;
 constexpr size_t kStageBytes = 104 * 1024;     // shared-memory slice per CTA
+constexpr int kLut = 256;                      // binning lookup-table entries
 
 struct DiscParams {
   int type;              // 1 bond, 2 angle, 3 torsion
@@ -95,6 +96,7 @@ __device__ __forceinline__ int ref_bin(float x, int dpind, double c, double lo,
 // pred monotone (false...true) and pred(b) true.
 template <class Pred>
 __device__ float bisect_first(float a, float b, Pred pred) {
+  if (a == 0.0f) a = 0.0f;   // -0 would order below every positive float's bits
   int lo = __float_as_int(a), hi = __float_as_int(b);
   if (pred(a)) return a;
   // invariant: pred(lo) false, pred(hi) true
@@ -113,6 +115,7 @@ __device__ float bisect_first(float a, float b, Pred pred) {
 // double expression is usually within a few floats of the threshold.
 template <class Pred>
 __device__ float bisect_guess(float a, float b, float guess, Pred pred) {
+  if (a == 0.0f) a = 0.0f;
   int ga = __float_as_int(a), gb = __float_as_int(b);
   int g = __float_as_int(fminf(fmaxf(guess, a), b));
   for (int span = 4; span <= 256; span *= 64) {
@@ -130,41 +133,45 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 }
 
 // --- block reductions -------------------------------------------------------
-__device__ float block_min(float v, float *red) {
-  for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    v = (threadIdx.x < blockDim.x / 32) ? red[threadIdx.x] : FLT_MAX;
-    for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+// One block-wide reduction of NM minima, NM maxima, a double sum and an OR
+// flag (one barrier round instead of one per value); results valid in thread 0.
+template <int NM>
+__device__ void block_minmax(float (&mn)[NM], float (&mx)[NM], double &sum, int &flag,
+                             float *red /*[2*NM][32]*/, double *redd /*[32]*/,
+                             int *redb /*[32]*/) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NM; ++q)
+    for (int o = 16; o; o >>= 1) {
+      mn[q] = fminf(mn[q], __shfl_xor_sync(0xffffffffu, mn[q], o));
+      mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], o));
+    }
+  for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  flag = __any_sync(0xffffffffu, flag) ? 1 : 0;
+  if (l == 0) {
+#pragma unroll
+    for (int q = 0; q < NM; ++q) {
+      red[q * 32 + w] = mn[q];
+      red[(NM + q) * 32 + w] = mx[q];
+    }
+    redd[w] = sum;
+    redb[w] = flag;
   }
-  return v;  // valid in thread 0
-}
-__device__ float block_max(float v, float *red) {
-  for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   __syncthreads();
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    v = (threadIdx.x < blockDim.x / 32) ? red[threadIdx.x] : -FLT_MAX;
-    for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (w == 0) {
+#pragma unroll
+    for (int q = 0; q < NM; ++q) {
+      mn[q] = l < nw ? red[q * 32 + l] : FLT_MAX;
+      mx[q] = l < nw ? red[(NM + q) * 32 + l] : -FLT_MAX;
+      for (int o = 16; o; o >>= 1) {
+        mn[q] = fminf(mn[q], __shfl_xor_sync(0xffffffffu, mn[q], o));
+        mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xffffffffu, mx[q], o));
+      }
+    }
+    sum = l < nw ? redd[l] : 0.0;
+    for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    flag = __any_sync(0xffffffffu, l < nw ? redb[l] : 0) ? 1 : 0;
   }
-  return v;
-}
-__device__ double block_sum(double v, double *red) {
-  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    v = (threadIdx.x < blockDim.x / 32) ? red[threadIdx.x] : 0.0;
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  }
-  return v;
 }
 
 struct DofState {
@@ -197,7 +204,8 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
   // thresholds after the staged slice: [scheme][side][k], k = 0..255
   float *thr = reinterpret_cast<float *>(dyn + (P.staged ? P.slice * 4 : 0));
   __shared__ Partial part[2];   // [0]: first reduction, [1]: displacement pass
-  __shared__ float redf[32];
+  __shared__ uint32_t lut_code[kLut];   // binning lookup table (per scheme)
+  __shared__ float lut_t[kLut];
   __shared__ double redd[32];
   __shared__ DofState st;
 
@@ -205,7 +213,13 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
   // fit thresholds in shared memory: the lanes of a warp index them by
   // their own coarse bin, which would serialise on the constant bank
   __shared__ float tfit_s[kMaxFit + 1];
-  for (int i = tid; i < kMaxFit; i += blockDim.x) part[0].hist[i] = 0;
+  // coarse occupancy counted in four copies (warps 4g..4g+3 use copy g) to
+  // spread the same-bin atomics of clustered torsions
+  __shared__ unsigned fithist[4][kMaxFit];
+  for (int i = tid; i < kMaxFit; i += blockDim.x) {
+    part[0].hist[i] = 0;
+    fithist[1][i] = fithist[2][i] = fithist[3][i] = 0;
+  }
   if (P.type == 3 && P.optimize)
     for (int i = tid; i <= P.nfit; i += blockDim.x) tfit_s[i] = P.tfit[i];
   __syncthreads();
@@ -241,7 +255,8 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
         k = min(max(k, 0), P.nfit - 1);
         while (k > 0 && x < tfit_s[k]) --k;
         while (k < P.nfit - 1 && x >= tfit_s[k + 1]) ++k;
-        atomicAdd(&part[0].hist[k], 1u);
+        const int copy = (threadIdx.x >> 7) & 3;
+        atomicAdd(copy ? &fithist[copy][k] : &part[0].hist[k], 1u);
       }
     }
   };
@@ -283,17 +298,30 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
   }
   const float *src = P.staged ? stage : gsrc;
 
-  float r;
-  r = block_min(xmin, redf); if (tid == 0) part[0].xmin = r;
-  r = block_max(xmax, redf); if (tid == 0) part[0].xmax = r;
-  r = block_min(cmin0, redf); if (tid == 0) part[0].cmin[0] = r;
-  r = block_max(cmax0, redf); if (tid == 0) part[0].cmax[0] = r;
-  r = block_min(cmin1, redf); if (tid == 0) part[0].cmin[1] = r;
-  r = block_max(cmax1, redf); if (tid == 0) part[0].cmax[1] = r;
-  double ds = block_sum((double)s_hi + (double)s_lo, redd);
-  if (tid == 0) part[0].sum = ds;
-  int anybad = __syncthreads_or(bad);
-  if (tid == 0) part[0].bad = anybad;
+  __shared__ float redm[6][32];
+  __shared__ int redb[32];
+  {
+    float mn[3] = {xmin, cmin0, cmin1}, mx[3] = {xmax, cmax0, cmax1};
+    double ds = (double)s_hi + (double)s_lo;
+    int anybad = bad;
+    block_minmax<3>(mn, mx, ds, anybad, &redm[0][0], redd, redb);
+    if (tid == 0) {
+      part[0].xmin = mn[0];
+      part[0].xmax = mx[0];
+      part[0].cmin[0] = mn[1];
+      part[0].cmax[0] = mx[1];
+      part[0].cmin[1] = mn[2];
+      part[0].cmax[1] = mx[2];
+      part[0].sum = ds;
+      part[0].bad = anybad;
+    }
+    if (is_tor && P.optimize) {
+      // fold the per-warp-group copies of the coarse occupancy into copy 0
+      __syncthreads();
+      for (int k = tid; k < P.nfit; k += blockDim.x)
+        part[0].hist[k] += fithist[1][k] + fithist[2][k] + fithist[3][k];
+    }
+  }
   cluster.sync();
 
   // ---- combine the cluster's partials (every CTA, same order) ------------
@@ -348,21 +376,46 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
           minidx = j;
         }
     } else {
-      int j = 0;
-      while (j < nf && hist_all[j] != 0) ++j;
-      minidx = j;
-      unsigned run = 0, best = 0;
-      for (int q = j; q < 2 * nf; ++q) {
-        bool empty = (hist_all[q % nf] == 0);
-        if (empty) {
-          run++;
-        } else {
-          if (run > best) {
-            minidx = q - (int)run;
-            best = run;
-          }
-          run = 0;
+      // Scan the doubled ring from the first empty bin; a run of empty bins
+      // is scored when the next non-empty bin closes it, the first strictly
+      // longest run wins (a run still open at the end is not scored).  The
+      // occupancy is walked run by run over bit words, not bin by bin.
+      const int n2 = 2 * nf;
+      auto occupied = [&](int q) { return hist_all[q % nf] != 0; };
+      auto word_ne = [&](int w) {   // occupancy bits q = 32w .. 32w+31 (q < n2)
+        unsigned m = 0;
+        for (int b = 0; b < 32; ++b) {
+          const int q = 32 * w + b;
+          if (q < n2 && occupied(q)) m |= 1u << b;
         }
+        return m;
+      };
+      unsigned ne[(2 * kMaxFit + 31) / 32];
+      const int nw = (n2 + 31) / 32;
+      for (int w = 0; w < nw; ++w) ne[w] = word_ne(w);
+      // first q >= from whose occupancy equals `want` (n2 if none)
+      auto next = [&](int from, bool want) {
+        for (int w = from >> 5; w < nw; ++w) {
+          unsigned m = want ? ne[w] : ~ne[w];
+          if (w == (from >> 5)) m &= ~0u << (from & 31);
+          if (w == nw - 1 && (n2 & 31)) m &= (1u << (n2 & 31)) - 1u;
+          if (m) return 32 * w + __ffs(m) - 1;
+        }
+        return n2;
+      };
+      const int j = next(0, false);   // first empty bin (nempty > 0)
+      minidx = j;
+      int best = 0;
+      for (int q = j; q < n2;) {
+        const int e = next(q, false);
+        if (e >= n2) break;
+        const int c = next(e, true);
+        if (c >= n2) break;
+        if (c - e > best) {
+          best = c - e;
+          minidx = e;
+        }
+        q = c;
       }
     }
     if (minidx >= nf) minidx = nf - 1;  // unreachable for valid occupancy
@@ -391,10 +444,18 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
         b0 = fmaxf(b0, x);
       }
     }
-    r = block_min(a0, redf); if (tid == 0) part[0].dmin[0] = r;
-    r = block_max(b0, redf); if (tid == 0) part[0].dmax[0] = r;
-    r = block_min(a1, redf); if (tid == 0) part[0].dmin[1] = r;
-    r = block_max(b1, redf); if (tid == 0) part[0].dmax[1] = r;
+    {
+      float mn[2] = {a0, a1}, mx[2] = {b0, b1};
+      double dummy = 0.0;
+      int nf = 0;
+      block_minmax<2>(mn, mx, dummy, nf, &redm[0][0], redd, redb);
+      if (tid == 0) {
+        part[0].dmin[0] = mn[0];
+        part[0].dmax[0] = mx[0];
+        part[0].dmin[1] = mn[1];
+        part[0].dmax[1] = mx[1];
+      }
+    }
     cluster.sync();
     if (tid == 0) {
       float d0n = FLT_MAX, d0x = -FLT_MAX, d1n = FLT_MAX, d1x = -FLT_MAX;
@@ -497,28 +558,35 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
     st.hi = hi;
     st.avg = avg;
     st.phase = phase;
-    for (int s = 0; s < P.nschemes; ++s) {
-      const int nb = P.schemes[s];
-      const double w = __ddiv_rn(__dsub_rn(hi, lo), (double)nb);
-      for (int side = 0; side < 2; ++side) {
-        if (!st.has[side]) {
-          st.kmin[s][side] = 0;
-          st.kmax[s][side] = -1;
-          continue;
-        }
-        int a = ref_bin(st.clsmin[side], dpind, c, lo, w);
-        int b = ref_bin(st.clsmax[side], dpind, c, lo, w);
-        st.kmin[s][side] = a;
-        st.kmax[s][side] = b;
-        if (a < 0 || b > nb) st.bad = 1;
-      }
+  }
+  __syncthreads();
+  // bin range of each side per scheme: one thread per (scheme, side, end)
+  __shared__ int kbad;
+  if (tid == 0) kbad = 0;
+  __syncthreads();
+  if (tid < 4 * P.nschemes) {
+    const int s = tid >> 2, side = (tid >> 1) & 1, end = tid & 1;
+    const int nb = P.schemes[s];
+    if (!st.has[side]) {
+      if (end == 0) st.kmin[s][side] = 0;
+      else st.kmax[s][side] = -1;
+    } else {
+      const double w = __ddiv_rn(__dsub_rn(st.hi, st.lo), (double)nb);
+      const int k = ref_bin(end ? st.clsmax[side] : st.clsmin[side], st.dpind, st.c, st.lo, w);
+      if (end == 0) st.kmin[s][side] = k;
+      else st.kmax[s][side] = k;
+      if ((end == 0 && k < 0) || (end == 1 && k > nb)) atomicOr(&kbad, 1);
     }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (kbad) st.bad = 1;
     if (rank == 0 && !st.bad) {
       double *e = extremes + 4 * dof;
-      e[0] = lo;
-      e[1] = hi;
-      e[2] = avg;
-      e[3] = (P.type == 3) ? phase : 0.0;
+      e[0] = st.lo;
+      e[1] = st.hi;
+      e[2] = st.avg;
+      e[3] = (P.type == 3) ? st.phase : 0.0;
     }
   }
   __syncthreads();
@@ -588,6 +656,78 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
       while (k < kmax && x >= t[k + 1]) ++k;
       return (uint32_t)((k == nb) ? nb - 1 : k) & 0xFFu;
     };
+    // ---- lookup table over the DOF's raw range --------------------------
+    // entry e(x) = floor((x - xlo) * L / (xhi - xlo)) in FP32 is a
+    // non-decreasing function of x, so each entry is an interval of floats.
+    // Inside an interval that does not hold the fold point, bin_of is
+    // non-decreasing; when it rises by at most one there, the entry keeps the
+    // two bins and the first float of the upper one, and a frame's bin is one
+    // compare.  Other entries (two or more rises, or the fold) fall back to
+    // bin_of per frame.  Bins are the same as bin_of's by construction.
+    const float xlo = (part[1].xmin == 0.0f) ? 0.0f : part[1].xmin, xhi = part[1].xmax;
+    const float lscale = (xhi > xlo) ? (float)kLut / (xhi - xlo) : 0.0f;
+    auto entry_of = [&](float x) -> int {
+      const int e = (int)__fmul_rn(__fsub_rn(x, xlo), lscale);
+      return min(e, kLut - 1);
+    };
+    __syncthreads();   // the previous scheme's frames are done with the table
+    for (int e = tid; e < kLut; e += blockDim.x) {
+      // first float of entry e (xhi + 1 ulp when the entry is empty)
+      float a;
+      if (e == 0) {
+        a = xlo;
+      } else if (entry_of(xhi) < e) {
+        a = __int_as_float(__float_as_int(xhi) + 1);
+      } else {
+        int l = __float_as_int(xlo), h = __float_as_int(xhi);   // e(l) < e <= e(h)
+        while (h - l > 1) {
+          const int m = l + ((h - l) >> 1);
+          if (entry_of(__int_as_float(m)) >= e) h = m; else l = m;
+        }
+        a = __int_as_float(h);
+      }
+      lut_t[e] = a;
+    }
+    __syncthreads();
+    uint32_t my_code[(kLut + 255) / 256];
+    float my_t[(kLut + 255) / 256];
+    for (int e = tid, q = 0; e < kLut; e += blockDim.x, ++q) {
+      const float a = lut_t[e];
+      const float b = (e + 1 < kLut) ? __int_as_float(__float_as_int(lut_t[e + 1]) - 1) : xhi;
+      uint32_t code = 0;
+      float t = INFINITY;
+      if (a <= b && a <= xhi) {
+        const uint32_t k0 = bin_of(a), k1 = bin_of(b);
+        const bool fold = dpind != 0 && a < xfold && xfold <= b;
+        if (fold || k1 > k0 + 1) {
+          code = 0x10000u;
+        } else if (k1 == k0) {
+          code = k0 | (k0 << 8);
+        } else {
+          int l = __float_as_int(a), h = __float_as_int(b);   // bin(l) = k0, bin(h) = k1
+          while (h - l > 1) {
+            const int m = l + ((h - l) >> 1);
+            if (bin_of(__int_as_float(m)) >= k1) h = m; else l = m;
+          }
+          code = k0 | (k1 << 8);
+          t = __int_as_float(h);
+        }
+      }
+      my_code[q] = code;
+      my_t[q] = t;
+    }
+    __syncthreads();
+    for (int e = tid, q = 0; e < kLut; e += blockDim.x, ++q) {
+      lut_code[e] = my_code[q];
+      lut_t[e] = my_t[q];
+    }
+    __syncthreads();
+    auto fast_bin = [&](float x) -> uint32_t {
+      const int e = entry_of(x);
+      const uint32_t code = lut_code[e];
+      if (code & 0x10000u) return bin_of(x);
+      return (x >= lut_t[e]) ? (code >> 8) & 0xFFu : code & 0xFFu;
+    };
     const bool vout = ((n & 15) == 0) && ((f0 & 15) == 0);
     if (vout) {
       uint64_t n16 = cnt >> 4;
@@ -597,15 +737,15 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           float4 v = reinterpret_cast<const float4 *>(xs)[q];
-          w4[q] = bin_of(v.x) | (bin_of(v.y) << 8) | (bin_of(v.z) << 16) |
-                  (bin_of(v.w) << 24);
+          w4[q] = fast_bin(v.x) | (fast_bin(v.y) << 8) | (fast_bin(v.z) << 16) |
+                  (fast_bin(v.w) << 24);
         }
         reinterpret_cast<uint4 *>(out)[g] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
       }
       for (uint64_t i = (n16 << 4) + tid; i < cnt; i += blockDim.x)
-        out[i] = (uint8_t)bin_of(src[i]);
+        out[i] = (uint8_t)fast_bin(src[i]);
     } else {
-      for (uint64_t i = tid; i < cnt; i += blockDim.x) out[i] = (uint8_t)bin_of(src[i]);
+      for (uint64_t i = tid; i < cnt; i += blockDim.x) out[i] = (uint8_t)fast_bin(src[i]);
     }
   }
 }

@@ -59,6 +59,29 @@ def test_discretize_synthetic_vs_oracle(gpu, orc, nframes):
                 np.testing.assert_allclose(ge[:, 2], oe[:, 2], rtol=1e-12)
 
 
+def test_discretize_edge_values_vs_oracle(gpu, orc):
+    """Signed zeros, exact zeros, constant DOFs, wide uniform ranges and
+    values on a single float: the binning table's edge cases."""
+    rng = np.random.default_rng(11)
+    n = 40_000
+    rows = {
+        1: [np.abs(rng.normal(0, 1e-3, n)), rng.uniform(0.0, 9.0, n), np.full(n, 1.5),
+            np.where(rng.random(n) < 0.5, 0.0, 1.25)],
+        2: [rng.uniform(0.0, np.pi, n), np.full(n, 2.0), np.where(rng.random(n) < 0.3, 0.0, 1.0)],
+        3: [rng.uniform(0.0, 2 * np.pi, n), np.where(rng.random(n) < 0.5, 0.0, 3.0),
+            np.mod(rng.vonmises(0.0, 2.0, n), 2 * np.pi)],
+    }
+    for typ, rs in rows.items():
+        x = np.stack(rs).astype(np.float32)
+        x[:, ::97] = np.float32(-0.0)
+        for sch in ([30], [255, 16]):
+            for opt in ((True, False) if typ == 3 else (True,)):
+                gb, ge = gpu.discretize(typ, x, sch, bins_ref=sch[0], optimize=opt)
+                ob, oe = orc.discretize(typ, x, sch, bins_ref=sch[0], optimize=opt)
+                assert np.array_equal(gb, ob), (typ, sch, opt)
+                assert np.array_equal(ge[:, [0, 1, 3]], oe[:, [0, 1, 3]])
+
+
 def test_discretize_rejects_out_of_domain(gpu):
     x = np.full((2, 64), 1.0, np.float32)
     x[1, 5] = 7.0   # torsion >= 2pi
