@@ -140,6 +140,9 @@ _SIGS = {
     "centre_gpu_screen_dev": (C.c_int, [_vp, C.POINTER(EntropyParams), C.POINTER(ScreenParams),
                                         C.c_uint32, _vp, _vp, _vp, _vp, _vp, C.c_uint64, _vp,
                                         C.POINTER(C.c_uint64)]),
+    "centre_gpu_screen": (C.c_int, [_vp, C.POINTER(EntropyParams), C.POINTER(ScreenParams),
+                                    C.c_uint32, _vp, _vp, _vp, _vp, _vp, C.c_uint64, _vp,
+                                    C.POINTER(C.c_uint64)]),
     "centre_gpu_screen_mlp_grad": (C.c_int, [_vp, _vp, C.c_uint64, _vp, _vp, _vp, _vp,
                                              C.POINTER(C.c_double)]),
 }

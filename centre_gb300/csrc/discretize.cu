@@ -704,13 +704,12 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
         } else if (k1 == k0) {
           code = k0 | (k0 << 8);
         } else {
-          int l = __float_as_int(a), h = __float_as_int(b);   // bin(l) = k0, bin(h) = k1
-          while (h - l > 1) {
-            const int m = l + ((h - l) >> 1);
-            if (bin_of(__int_as_float(m)) >= k1) h = m; else l = m;
-          }
+          // one rise inside one side: it happens at that side's threshold
+          // for bin k1 (the first float whose bin is >= k1; k1 <= nb - 1
+          // here, so the nb -> nb - 1 fold of the top bin is not involved)
+          const int side = (dpind != 0 && a >= xfold) ? 1 : 0;
           code = k0 | (k1 << 8);
-          t = __int_as_float(h);
+          t = (side ? t1 : t0)[k1];
         }
       }
       my_code[q] = code;
@@ -728,6 +727,26 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
       if (code & 0x10000u) return bin_of(x);
       return (x >= lut_t[e]) ? (code >> 8) & 0xFFu : code & 0xFFu;
     };
+    // four frames at once: table reads first, rare slow entries after
+    auto bins4 = [&](float4 v) -> uint32_t {
+      const float xs[4] = {v.x, v.y, v.z, v.w};
+      uint32_t code[4];
+      float tt[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = entry_of(xs[u]);
+        code[u] = lut_code[e];
+        tt[u] = lut_t[e];
+      }
+      uint32_t w = 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        uint32_t b = (xs[u] >= tt[u]) ? (code[u] >> 8) & 0xFFu : code[u] & 0xFFu;
+        if (code[u] & 0x10000u) b = bin_of(xs[u]);
+        w |= b << (8 * u);
+      }
+      return w;
+    };
     const bool vout = ((n & 15) == 0) && ((f0 & 15) == 0);
     if (vout) {
       uint64_t n16 = cnt >> 4;
@@ -737,8 +756,7 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           float4 v = reinterpret_cast<const float4 *>(xs)[q];
-          w4[q] = fast_bin(v.x) | (fast_bin(v.y) << 8) | (fast_bin(v.z) << 16) |
-                  (fast_bin(v.w) << 24);
+          w4[q] = bins4(v);
         }
         reinterpret_cast<uint4 *>(out)[g] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
       }

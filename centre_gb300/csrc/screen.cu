@@ -792,3 +792,27 @@ extern "C" int centre_gpu_screen_dev(centre_ctx *ctx, const centre_entropy_param
   CENTRE_CUDA(ctx, cudaStreamSynchronize(st));
   return CENTRE_OK;
 }
+
+extern "C" int centre_gpu_screen(centre_ctx *ctx, const centre_entropy_params *p,
+                                 const centre_screen_params *sp, uint32_t ndof,
+                                 const uint8_t *types, const uint8_t *bins,
+                                 const double *extremes, float *weights, float *losses,
+                                 uint64_t capacity, uint32_t *pairs, uint64_t *npairs) {
+  if (!ctx || !p || !sp || !types || !bins || !extremes || !pairs || !npairs)
+    return set_error(ctx, CENTRE_E_ARG, "screen: null argument");
+  cudaSetDevice(ctx->device);
+  const uint64_t nbytes = (uint64_t)ndof * p->nschemes * p->nframes;
+  Buf dt, db, de, dp;
+  CENTRE_TRY(dalloc(ctx, dt, ndof));
+  CENTRE_TRY(dalloc(ctx, db, nbytes));
+  CENTRE_TRY(dalloc(ctx, de, sizeof(double) * 4 * ndof));
+  CENTRE_TRY(dalloc(ctx, dp, sizeof(uint32_t) * 2 * std::max<uint64_t>(capacity, 1)));
+  CENTRE_CUDA(ctx, cudaMemcpy(dt.p, types, ndof, cudaMemcpyHostToDevice));
+  CENTRE_CUDA(ctx, cudaMemcpy(db.p, bins, nbytes, cudaMemcpyHostToDevice));
+  CENTRE_CUDA(ctx, cudaMemcpy(de.p, extremes, sizeof(double) * 4 * ndof, cudaMemcpyHostToDevice));
+  CENTRE_TRY(centre_gpu_screen_dev(ctx, p, sp, ndof, (const uint8_t *)dt.p, (const uint8_t *)db.p,
+                                   (const double *)de.p, weights, losses, capacity,
+                                   (uint32_t *)dp.p, npairs));
+  CENTRE_CUDA(ctx, cudaMemcpy(pairs, dp.p, sizeof(uint32_t) * 2 * *npairs, cudaMemcpyDeviceToHost));
+  return CENTRE_OK;
+}

@@ -2,6 +2,7 @@
 // with the three stages running on the GPU library.
 //
 //   centre_gpu -i input.cfg [-O] [--device N] [--print-inputs]
+//              [--learned-neighbours K]
 //
 // Same input file and output files as the reference.  Errors end the run
 // with a non-zero exit status (the reference exits with status 0 after
@@ -43,7 +44,11 @@ void usage() {
                "                 [vonmiseskde] [entropy] sections, as for centre_OMP)\n"
                "  -O             overwrite existing output files\n"
                "  --device N     CUDA device (default 0)\n"
-               "  --print-inputs parse and print the inputs, then stop\n";
+               "  --print-inputs parse and print the inputs, then stop\n"
+               "  --learned-neighbours K\n"
+               "                 choose K partners per DOF with the learned pair screen\n"
+               "                 (after discretisation) instead of a neighbor file; the\n"
+               "                 lists are written to outfilepath/neigh_learned.txt\n";
 }
 
 bool exists(const std::string &p) {
@@ -122,6 +127,13 @@ int main(int argc, char **argv) {
   };
   Discretizer discretizer(in, gpu);
   if (!stage("Discretization", [&](std::string *e) { return discretizer.run(e); })) return 5;
+  if (const char *k = arg_value(argc, argv, "--learned-neighbours")) {
+    const std::string path = out_path(in, "neigh_learned.txt");
+    if (!stage("Pair screen", [&](std::string *e) {
+          return learn_neighbours(in, gpu, (uint32_t)std::atoi(k), path, e);
+        }))
+      return 5;
+  }
   EntropyCalculator calculator(in, gpu);
   if (!stage("Entropy calculation", [&](std::string *e) { return calculator.run(e); })) return 5;
   EntropyScorer scorer(in, gpu);

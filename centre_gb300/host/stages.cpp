@@ -459,6 +459,76 @@ bool EntropyCalculator::run(std::string *err) {
   return true;
 }
 
+// ------------------------------------------------------ learned neighbours --
+bool learn_neighbours(Inputs &in, Gpu &gpu, uint32_t nneigh, const std::string &path,
+                      std::string *err) {
+  const uint32_t ws = in.entropy.workset;
+  const Subset &ss = in.subset;
+  TypeBins tb[3];
+  if (!load_type(in, 1, ss.bonds, tb[0], err) || !load_type(in, 2, ss.angles, tb[1], err) ||
+      !load_type(in, 3, ss.torsions, tb[2], err))
+    return false;
+  std::vector<uint8_t> types, bins;
+  std::vector<double> ext;
+  std::vector<std::pair<int, uint32_t>> who;   // (type index, DOF id) per array slot
+  for (int t = 0; t < 3; ++t) {
+    for (uint32_t id : tb[t].ids) {
+      types.push_back((uint8_t)(t + 1));
+      who.push_back({t, id});
+    }
+    bins.insert(bins.end(), tb[t].bins.begin(), tb[t].bins.end());
+    ext.insert(ext.end(), tb[t].ext.begin(), tb[t].ext.end());
+  }
+  const uint32_t ndof = (uint32_t)types.size();
+  if (ndof < 3) return fail(err, "learned neighbours need at least 3 DOFs");
+  centre_entropy_params p = make_params(in);
+  centre_screen_params sp;
+  memset(&sp, 0, sizeof(sp));
+  sp.feat_div = 5;
+  const uint64_t all = (uint64_t)ndof * (ndof - 1) / 2;
+  sp.ntrain = (uint32_t)std::min<uint64_t>(200000, std::max<uint64_t>(4096, all));
+  sp.batch = std::min<uint32_t>(4096, sp.ntrain);
+  sp.nneigh = std::min<uint32_t>(nneigh, ndof - 1);
+  sp.nprefilter = std::min<uint32_t>(std::max<uint32_t>(4 * sp.nneigh, 64), 1024);
+  sp.nprefilter = std::max(sp.nprefilter, sp.nneigh);
+  sp.epochs = 3;
+  sp.lr = 2e-3f;
+  sp.train = 1;
+  sp.init_weights = 1;
+  sp.seed = in.bats.randseed ? in.bats.randseed : 17;
+  std::vector<float> w(CENTRE_SCREEN_NPARAMS);
+  const uint64_t cap = (uint64_t)ndof * sp.nneigh;
+  std::vector<uint32_t> pairs(2 * cap);
+  uint64_t npairs = 0;
+  const int rc = centre_gpu_screen(gpu.ctx(), &p, &sp, ndof, types.data(), bins.data(),
+                                   ext.data(), w.data(), nullptr, cap, pairs.data(), &npairs);
+  if (rc != CENTRE_OK) return fail(err, gpu.error(rc, "pair screen"));
+  // array order is bonds, angles, torsions: i < j puts the lower type first
+  Neighbours nb;
+  std::map<uint32_t, std::vector<uint32_t>> *block[3][3] = {
+      {&nb.bb, &nb.ba, &nb.bd}, {nullptr, &nb.aa, &nb.ad}, {nullptr, nullptr, &nb.dd}};
+  const uint32_t need[3][3] = {{kBB2D, kBA2D, kBD2D}, {0, kAA2D, kAD2D}, {0, 0, kDD2D}};
+  for (uint64_t q = 0; q < npairs; ++q) {
+    const auto a = who[pairs[2 * q]], b = who[pairs[2 * q + 1]];
+    if (!(ws & need[a.first][b.first])) continue;
+    (*block[a.first][b.first])[a.second].push_back(b.second);
+  }
+  std::ofstream o(path.c_str());
+  const char *kind[6] = {"bond", "angle", "torsion", "bacross", "bdcross", "adcross"};
+  const std::map<uint32_t, std::vector<uint32_t>> *maps[6] = {&nb.bb, &nb.aa, &nb.dd,
+                                                               &nb.ba, &nb.bd, &nb.ad};
+  for (int k = 0; k < 6; ++k)
+    for (const auto &kv : *maps[k]) {
+      o << kind[k] << " " << kv.first << " " << kv.second.size();
+      for (uint32_t v : kv.second) o << " " << v;
+      o << ";\n";
+    }
+  if (!o) return fail(err, "cannot write " + path);
+  in.neighbours = nb;
+  in.entropy.useneighbor = true;
+  return true;
+}
+
 // ----------------------------------------------------------- EntropyScorer --
 bool EntropyScorer::run(std::string *err) {
   if (!in_.control.genconvgdata) return true;

@@ -69,6 +69,14 @@ class EntropyScorer {
   Gpu &gpu_;
 };
 
+// Neighbour lists chosen from the data by the learned pair screen
+// (centre_gpu_screen) instead of a neighbor file: reads the bin files, keeps
+// `nneigh` partners per DOF, replaces `inputs.neighbours` and writes the
+// lists to `path` in the reference's neighbour-file grammar
+// (src/Centre.cpp:459-593) so the reference can score the same pairs.
+bool learn_neighbours(Inputs &inputs, Gpu &gpu, uint32_t nneigh, const std::string &path,
+                      std::string *err);
+
 // File helpers shared with the command-line tool.
 std::string out_path(const Inputs &in, const std::string &name);
 

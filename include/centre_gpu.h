@@ -303,6 +303,13 @@ int centre_gpu_screen_dev(centre_ctx *ctx, const centre_entropy_params *p,
                           const double *extremes, float *weights, float *losses,
                           uint64_t capacity, uint32_t *pairs, uint64_t *npairs);
 
+/* The same with host inputs and a host pair list [capacity][2]. */
+int centre_gpu_screen(centre_ctx *ctx, const centre_entropy_params *p,
+                      const centre_screen_params *sp, uint32_t ndof,
+                      const uint8_t *types, const uint8_t *bins,
+                      const double *extremes, float *weights, float *losses,
+                      uint64_t capacity, uint32_t *pairs, uint64_t *npairs);
+
 /* One forward and backward pass of the screen network over n samples
  * (host arrays): feats [n][12], targets [n]; pred [n] (may be NULL), grad
  * [CENTRE_SCREEN_NPARAMS] of the mean squared error, *loss that error.

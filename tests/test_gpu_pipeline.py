@@ -219,3 +219,56 @@ def test_pipeline_vonmises_kde(gpu, tmp_path):
         assert f[0] == "torsion" and int(f[1]) == d and int(f[2]) == nfound[d]
         assert [float(x) for x in f[3:]] == pytest.approx(minima[d, : nfound[d]], abs=1e-8)
     assert os.path.exists(out / "Tree-MIST-ML_b-3_s-1.csv")
+
+
+def test_pipeline_learned_neighbours(gpu, tmp_path):
+    """--learned-neighbours K: the pair screen replaces the neighbour file;
+    its lists are written in the reference's neighbour-file grammar, the
+    entropy files hold exactly those pairs, and A-MIST stays close to the
+    all-pairs MIST of the same trajectory."""
+    tr = chain_trajectory(40, 20000, seed=31, coupling="block8")
+    body = """    nsteps = 4
+[discretization]
+    fname = traj_bat.nc
+[histogram]
+    nbins = 30
+[entropy]
+    workset = 2D
+    estimator = ML
+    scoringmethod = MIST
+"""
+    (tmp_path / "full").mkdir()
+    full_dir = case(tmp_path / "full", tr, body)
+    learned = tmp_path / "learned"
+    learned.mkdir()
+    (learned / "out").mkdir()
+    cdf5.write_bat(str(learned / "traj_bat.nc"), tr.bonds, tr.angles, tr.torsions)
+    cfg = learned / "in.cfg"
+    cfg.write_text(f"[control]\n    infilepath = {learned}/\n    outfilepath = {learned}/out/\n"
+                   + body)
+    r = subprocess.run([TOOL, "-i", str(cfg), "-O", "--learned-neighbours", "12"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = learned / "out"
+    # neighbour file grammar: "<kind> <key> <n> ids...;"
+    lists = {}
+    for chunk in open(out / "neigh_learned.txt").read().split(";"):
+        f = chunk.split()
+        if not f:
+            continue
+        kind, key, n = f[0], int(f[1]), int(f[2])
+        assert len(f) == 3 + n
+        lists.setdefault(kind, []).extend((key, int(v)) for v in f[3:])
+    files = {"bond": "bnd", "angle": "ang", "torsion": "tor", "bacross": "ba", "bdcross": "bd",
+             "adcross": "ad"}
+    total = 0
+    for kind, f in files.items():
+        ids, _ = cdf5.read_entcontri(str(out / f"entcontri_{f}-2d.nc"))
+        assert [tuple(x) for x in ids] == lists.get(kind, [])
+        total += len(ids)
+    ndof = 3 * 40 - 6
+    assert 0 < total <= ndof * 12
+    _, rows_full = read_csv(full_dir / "MIST-ML_convergence_b-30.csv")
+    _, rows_learn = read_csv(out / "MIST-ML_convergence_b-30.csv")
+    s_full, s_learn = float(rows_full[-1][-1]), float(rows_learn[-1][-1])
+    assert abs(s_learn - s_full) <= 0.01 * abs(s_full)
