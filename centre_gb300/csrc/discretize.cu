@@ -204,8 +204,13 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
   // thresholds after the staged slice: [scheme][side][k], k = 0..255
   float *thr = reinterpret_cast<float *>(dyn + (P.staged ? P.slice * 4 : 0));
   __shared__ Partial part[2];   // [0]: first reduction, [1]: displacement pass
-  __shared__ uint32_t lut_code[kLut];   // binning lookup table (per scheme)
-  __shared__ float lut_t[kLut];
+  // one buffer for two phases: per-warp coarse occupancy counters while the
+  // slice is scanned, the binning lookup table (per scheme) afterwards
+  constexpr int kFitWords = (kMaxFit + 1) / 2;   // two 16-bit counters a word
+  __shared__ uint32_t phase_buf[(kThreads / 32) * kFitWords > 2 * kLut
+                                    ? (kThreads / 32) * kFitWords : 2 * kLut];
+  uint32_t *lut_code = phase_buf;
+  float *lut_t = reinterpret_cast<float *>(phase_buf + kLut);
   __shared__ double redd[32];
   __shared__ DofState st;
 
@@ -213,13 +218,15 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
   // fit thresholds in shared memory: the lanes of a warp index them by
   // their own coarse bin, which would serialise on the constant bank
   __shared__ float tfit_s[kMaxFit + 1];
-  // coarse occupancy counted in four copies (warps 4g..4g+3 use copy g) to
-  // spread the same-bin atomics of clustered torsions
-  __shared__ unsigned fithist[4][kMaxFit];
-  for (int i = tid; i < kMaxFit; i += blockDim.x) {
-    part[0].hist[i] = 0;
-    fithist[1][i] = fithist[2][i] = fithist[3][i] = 0;
-  }
+  // coarse occupancy: a private histogram per warp (16-bit counters, two to
+  // a word; a warp sees at most 32 x slice/blockDim frames of a slice) so
+  // the same-bin atomics of clustered torsions stay inside one warp
+  uint32_t *warp_fit = phase_buf + (threadIdx.x >> 5) * kFitWords;
+  // a warp counts at most 32 * ceil(slice / blockDim) + 256 frames of its
+  // slice; beyond 16 bits the CTA-wide 32-bit counters are used directly
+  const bool small_fit = 32ull * ((P.slice + kThreads - 1) / kThreads) + 256 < 65536ull;
+  for (int i = tid; i < kMaxFit; i += blockDim.x) part[0].hist[i] = 0;
+  for (int i = tid; i < (kThreads / 32) * kFitWords; i += blockDim.x) phase_buf[i] = 0;
   if (P.type == 3 && P.optimize)
     for (int i = tid; i <= P.nfit; i += blockDim.x) tfit_s[i] = P.tfit[i];
   __syncthreads();
@@ -255,8 +262,8 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
         k = min(max(k, 0), P.nfit - 1);
         while (k > 0 && x < tfit_s[k]) --k;
         while (k < P.nfit - 1 && x >= tfit_s[k + 1]) ++k;
-        const int copy = (threadIdx.x >> 7) & 3;
-        atomicAdd(copy ? &fithist[copy][k] : &part[0].hist[k], 1u);
+        if (small_fit) atomicAdd(&warp_fit[k >> 1], (k & 1) ? 0x10000u : 1u);
+        else atomicAdd(&part[0].hist[k], 1u);
       }
     }
   };
@@ -316,10 +323,15 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
       part[0].bad = anybad;
     }
     if (is_tor && P.optimize) {
-      // fold the per-warp-group copies of the coarse occupancy into copy 0
+      // sum the per-warp counters into the CTA's occupancy
       __syncthreads();
-      for (int k = tid; k < P.nfit; k += blockDim.x)
-        part[0].hist[k] += fithist[1][k] + fithist[2][k] + fithist[3][k];
+      if (small_fit)
+        for (int k = tid; k < P.nfit; k += blockDim.x) {
+          unsigned c = 0;
+          for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            c += (phase_buf[w * kFitWords + (k >> 1)] >> ((k & 1) * 16)) & 0xFFFFu;
+          part[0].hist[k] = c;
+        }
     }
   }
   cluster.sync();
@@ -363,10 +375,25 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
   // ---- torsion displacement (largest empty circular run) -----------------
   __shared__ double disp_s;
   __shared__ float xdisp_s;
+  // occupancy of the doubled ring as bit words, built by warp 0 with ballots
+  __shared__ unsigned ne_s[(2 * kMaxFit + 31) / 32];
+  __shared__ unsigned nempty_s;
+  if (is_tor && P.optimize && tid < 32) {
+    const int nf = P.nfit, n2 = 2 * nf;
+    for (int w = 0; w < (n2 + 31) / 32; ++w) {
+      const int q = 32 * w + tid;
+      const unsigned m = __ballot_sync(0xffffffffu, q < n2 && hist_all[q % nf] != 0);
+      if (tid == 0) ne_s[w] = m;
+    }
+    unsigned e = 0;
+    for (int k = tid; k < nf; k += 32) e += (hist_all[k] == 0);
+    for (int o = 16; o; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if (tid == 0) nempty_s = e;
+  }
+  __syncthreads();
   if (is_tor && P.optimize && tid == 0) {
     const int nf = P.nfit;
-    unsigned nempty = 0;
-    for (int i = 0; i < nf; ++i) nempty += (hist_all[i] == 0);
+    const unsigned nempty = nempty_s;
     int minidx = 0;
     if (nempty == 0) {
       unsigned rec = hist_all[0];
@@ -381,18 +408,8 @@ discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
       // longest run wins (a run still open at the end is not scored).  The
       // occupancy is walked run by run over bit words, not bin by bin.
       const int n2 = 2 * nf;
-      auto occupied = [&](int q) { return hist_all[q % nf] != 0; };
-      auto word_ne = [&](int w) {   // occupancy bits q = 32w .. 32w+31 (q < n2)
-        unsigned m = 0;
-        for (int b = 0; b < 32; ++b) {
-          const int q = 32 * w + b;
-          if (q < n2 && occupied(q)) m |= 1u << b;
-        }
-        return m;
-      };
-      unsigned ne[(2 * kMaxFit + 31) / 32];
+      const unsigned *ne = ne_s;
       const int nw = (n2 + 31) / 32;
-      for (int w = 0; w < nw; ++w) ne[w] = word_ne(w);
       // first q >= from whose occupancy equals `want` (n2 if none)
       auto next = [&](int from, bool want) {
         for (int w = from >> 5; w < nw; ++w) {

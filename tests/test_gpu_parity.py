@@ -176,6 +176,33 @@ def test_entropy2d_explicit_pair_list_orientation(gpu, orc):
         np.testing.assert_allclose(s2, o, rtol=RTOL, atol=1e-13)
 
 
+@pytest.mark.parametrize("ndof,nframes,nsteps,nb", [
+    (2, 17, 4, 2),        # fewest DOFs, frames not divisible by steps
+    (3, 1003, 10, 255),   # largest bin count
+    (5, 4096, 1, 1),      # a single bin: every entropy from one cell
+    (7, 999, 7, 13),
+])
+def test_entropy_edge_sizes_vs_oracle(gpu, orc, ndof, nframes, nsteps, nb):
+    """Edge shapes of the count and entropy kernels against the oracle, all
+    four estimators, including a constant DOF (one occupied bin)."""
+    rng = np.random.default_rng(nframes + nb)
+    bins = rng.integers(0, nb, size=(ndof, 1, nframes), dtype=np.uint8)
+    bins[0, 0, :] = 0                                   # constant DOF
+    types = np.array([(1 + k % 3) for k in range(ndof)], np.uint8)
+    types.sort()
+    ext = np.tile(np.array([[0.5, 2.5, 1.5, 0.0]]), (ndof, 1))
+    ext[types == 3, 1] = 2 * np.pi
+    ext[types == 2, 1] = np.pi
+    ests = [0, 1, 2, 3]
+    p = make_params(nframes, nsteps, [nb], ests, True)
+    s1 = gpu.entropy1d(p, types, bins, ext)
+    o1 = orc.entropy1d(types, bins, ext, nsteps, [nb], ests, True)
+    np.testing.assert_allclose(s1, o1, rtol=RTOL, atol=1e-13)
+    s2 = gpu.entropy2d(p, types, bins, ext)
+    o2 = orc.entropy2d(all_pairs(ndof), types, bins, ext, nsteps, [nb], ests, True)
+    np.testing.assert_allclose(s2, o2, rtol=RTOL, atol=1e-13)
+
+
 def test_entropy2d_rejects_bad_bins(gpu):
     bins = np.zeros((3, 1, 1000), np.uint8)
     bins[1, 0, 10] = 40
