@@ -41,6 +41,22 @@ NSTEPS = 10
 PAIR_TRAFFIC_PER_PAIR = 76.0e6 / 176121
 
 
+def slowest_rank(value, dist, device="cpu"):
+    """The largest of every rank's value (a step time): the job runs as fast
+    as its slowest replica."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, step_s, world):
+    """Whole-job units per second: every rank processed its own units in a
+    step that lasted `step_s` (the slowest rank's)."""
+    return world * units_per_rank / step_s
+
+
 def workload(name):
     from centre_gb300.synth import WORKLOADS
     w = dict(WORKLOADS[name])
@@ -252,11 +268,8 @@ def run_ours(args):
     t_score, n_score = ctx.timer(3)
     ctx.enable_timing(False)
 
-    t = torch.tensor([step_ms], device=dev)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    step_ms = float(t.item())
-    value = world * npairs / (step_ms / 1e3)
+    step_ms = slowest_rank(step_ms, dist, dev)
+    value = job_throughput(npairs, step_ms / 1e3, world)
 
     hbm, bf16, src = peaks()
     fp8_peak = 2.0 * bf16
@@ -373,10 +386,7 @@ def run_e2e(ctx, tr, args, w, world, dist, dev):
     for _ in range(steps):
         step()
     dt = (time.perf_counter() - t0) / steps
-    t = torch.tensor([dt], device=dev)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    dt = float(t.item())
+    dt = slowest_rank(dt, dist, dev)
     h2d = sum(b.nbytes for _, b in blocks) + 2 * bins.nbytes + 2 * ext.nbytes + s1.nbytes \
         + s2.nbytes + 3 * types.nbytes
     d2h = bins.nbytes + ext.nbytes + s1.nbytes + s2.nbytes + mi.nbytes
@@ -467,10 +477,7 @@ def run_batch(args):
     launches = ctx.launches - launches0
     graph_ms, ngraph = ctx.timer(2)
     ctx.enable_timing(False)
-    t = torch.tensor([step_ms], device=dev)
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    step_ms = float(t.item())
+    step_ms = slowest_rank(step_ms, dist, dev)
     hbm, bf16, src = peaks()
     fp8_peak = 2.0 * bf16
     # tot_incr = sum over chains of pairs x frames used: 2*B^2 one-hot flops each

@@ -170,8 +170,29 @@ int counts_chunk(centre_ctx *ctx, const EntParams &E, int scheme, uint32_t ndof,
                  unsigned *d_counts) {
   const int nb = E.schemes[scheme];
   const int width = atomic_pair_width(nb);
-  if (!atomic_fits(nb))
-    return set_error(ctx, CENTRE_E_UNSUPPORTED, "bin count too large for shared-memory counts");
+  if (!atomic_fits(nb)) {
+    // histograms too large for shared memory: the global-histogram kernel
+    // over the chunk's pairs (uploaded as a device list)
+    int st2 = CENTRE_OK;
+    uint32_t *d_pl = (uint32_t *)scratch(ctx, kSlotPairs, sizeof(uint32_t) * 2 * (p1 - p0), &st2);
+    if (!d_pl) return st2;
+    CENTRE_CUDA(ctx, cudaMemcpyAsync(d_pl, h_pairs + 2 * p0, sizeof(uint32_t) * 2 * (p1 - p0),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+    PairParams P;
+    memset(&P, 0, sizeof(P));
+    P.bins = d_bins;
+    P.nframes = E.nframes;
+    P.step_size = E.step_size;
+    P.ndof = ndof;
+    P.nschemes = E.nschemes;
+    P.scheme = scheme;
+    P.nb = nb;
+    P.nsteps = E.nsteps;
+    CENTRE_TRY(launch_pairs_global(ctx, P, d_pl, 0, p1 - p0, (const double *)ctx->d_clnc,
+                                   nullptr, nullptr, d_counts));
+    CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CENTRE_OK;
+  }
   std::vector<PairTask> tasks;
   plan_tasks(h_pairs, p0, p1, width, tasks);
   int st = CENTRE_OK;
@@ -268,9 +289,12 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
       if (use_tc) {
         P.all_pairs = 1;
         CENTRE_TRY(launch_pairs_tc(ctx, P, d_tab, d_sclnc, d_nnz));
+      } else if (!atomic_fits(nb)) {
+        // histograms too large for shared memory: one global histogram per CTA
+        P.all_pairs = all ? 1 : 0;
+        CENTRE_TRY(launch_pairs_global(ctx, P, d_pairs, 0, npairs, d_tab, d_sclnc, d_nnz,
+                                       nullptr));
       } else {
-        if (!atomic_fits(nb))
-          return set_error(ctx, CENTRE_E_UNSUPPORTED, "bin count too large for shared-memory counts");
         if (all) {
           int ppair = atomic_pair_width(nb);
           int tile = 1;

@@ -508,6 +508,108 @@ pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nit
 }
 
 // ----------------------------------------------------------------------------
+// Joint counts for bin counts whose histograms do not fit shared memory
+// (more than 214 bins): each CTA owns one nb x nb histogram in global
+// memory (L2-resident) and counts a pair's frames into it with global
+// atomics, one pair at a time.  At every step it emits the pair's moments
+// (or copies the cumulative counts), then clears the histogram.  Reads of
+// the histogram bypass L1 (the atomics update L2).
+__global__ void __launch_bounds__(512)
+pairs_global_kernel(const uint8_t *__restrict__ bins, const __grid_constant__ PairParams P,
+                    const uint32_t *__restrict__ pairs, uint64_t p0, uint64_t np,
+                    const double *__restrict__ gtab, U128 *__restrict__ sclnc,
+                    unsigned *__restrict__ nnz, unsigned *__restrict__ counts,
+                    unsigned *__restrict__ hist_all, int *__restrict__ flag) {
+  const int nb = P.nb, nb2 = nb * nb;
+  unsigned *h = hist_all + (uint64_t)blockIdx.x * nb2;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  __shared__ U128 wacc[32];
+  __shared__ unsigned wnz[32];
+  int bad = 0;
+  for (uint64_t q = blockIdx.x; q < np; q += gridDim.x) {
+    const uint64_t gp = p0 + q;
+    uint32_t i, j;
+    if (pairs) {
+      i = pairs[2 * gp];
+      j = pairs[2 * gp + 1];
+    } else {
+      tri_pair(gp, P.ndof, i, j);
+    }
+    const uint8_t *bi = bins + ((uint64_t)i * P.nschemes + P.scheme) * P.nframes;
+    const uint8_t *bj = bins + ((uint64_t)j * P.nschemes + P.scheme) * P.nframes;
+    for (int t = 0; t < P.nsteps; ++t) {
+      const uint64_t f0 = (uint64_t)t * P.step_size, f1 = f0 + P.step_size;
+      for (uint64_t f = f0 + tid; f < f1; f += blockDim.x) {
+        const unsigned a = bi[f], b = bj[f];
+        if (a >= (unsigned)nb || b >= (unsigned)nb) {
+          bad = 1;
+          continue;
+        }
+        atomicAdd(&h[a * nb + b], 1u);
+      }
+      __syncthreads();
+      if (counts) {
+        unsigned *dst = counts + (q * P.nsteps + t) * (uint64_t)nb2;
+        for (int c = tid; c < nb2; c += blockDim.x) dst[c] = __ldcg(h + c);
+      } else {
+        U128 acc;
+        acc.lo = acc.hi = 0ull;
+        unsigned cz = 0;
+        for (int c = tid; c < nb2; c += blockDim.x) {
+          const unsigned v = __ldcg(h + c);
+          acc = u128_add(acc, u128_from_double(v < (unsigned)kTabGlobal ? __ldg(gtab + v)
+                                                                      : clnc_value(v)));
+          cz += (v != 0);
+        }
+        for (int off = 16; off; off >>= 1) {
+          acc = u128_add(acc, u128_shfl_xor(acc, off));
+          cz += __shfl_xor_sync(0xffffffffu, cz, off);
+        }
+        if (lane == 0) {
+          wacc[warp] = acc;
+          wnz[warp] = cz;
+        }
+        __syncthreads();
+        if (tid == 0) {
+          U128 tot = wacc[0];
+          unsigned z = wnz[0];
+          for (int w = 1; w < nwarps; ++w) {
+            tot = u128_add(tot, wacc[w]);
+            z += wnz[w];
+          }
+          sclnc[gp * P.nsteps + t] = tot;
+          nnz[gp * P.nsteps + t] = z;
+        }
+      }
+      __syncthreads();
+    }
+    for (int c = tid; c < nb2; c += blockDim.x) h[c] = 0u;
+    __threadfence_block();
+    __syncthreads();
+  }
+  if (bad) atomicOr(flag, kFlagBinRange);
+}
+
+int launch_pairs_global(centre_ctx *ctx, const PairParams &P, const uint32_t *d_pairs,
+                        uint64_t p0, uint64_t np, const double *d_tab, U128 *d_sclnc,
+                        unsigned *d_nnz, unsigned *d_counts) {
+  if (np == 0) return CENTRE_OK;
+  const uint64_t grid = std::min<uint64_t>(np, (uint64_t)ctx->sm_count * 4);
+  int st = CENTRE_OK;
+  unsigned *d_hist = (unsigned *)scratch(ctx, kSlotAux3,
+                                         sizeof(unsigned) * grid * (uint64_t)P.nb * P.nb, &st);
+  if (!d_hist) return st;
+  CENTRE_CUDA(ctx, cudaMemsetAsync(d_hist, 0, sizeof(unsigned) * grid * (uint64_t)P.nb * P.nb,
+                                   ctx->stream));
+  KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
+  pairs_global_kernel<<<(unsigned)grid, 512, 0, ctx->stream>>>(P.bins, P, d_pairs, p0, np, d_tab,
+                                                             d_sclnc, d_nnz, d_counts, d_hist,
+                                                             ctx->d_flag);
+  ctx->launches++;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  return CENTRE_OK;
+}
+
 // ----------------------------------------------------------------------------
 // S2 from the integer moments (ML, MM).  One thread per (pair, step) of a
 // scheme.

@@ -154,6 +154,9 @@ int pairs_hist_batch_occupancy(centre_ctx *ctx, int tile, int threads, int nb, i
 int launch_pairs_hist_batch(centre_ctx *ctx, const BatchSys *d_sys, int nsys, uint64_t nitems,
                             const BatchCommon &B, int tile, int threads, int grid,
                             const double *d_tab);
+int launch_pairs_global(centre_ctx *ctx, const PairParams &P, const uint32_t *d_pairs,
+                        uint64_t p0, uint64_t np, const double *d_tab, U128 *d_sclnc,
+                        unsigned *d_nnz, unsigned *d_counts);
 int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uint32_t *d_pairs,
                       int all_pairs, uint32_t ndof, const double *d_ext, const double *d_lsum,
                       const U128 *d_sclnc, const unsigned *d_nnz, uint64_t npairs,

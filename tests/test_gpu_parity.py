@@ -203,6 +203,23 @@ def test_entropy_edge_sizes_vs_oracle(gpu, orc, ndof, nframes, nsteps, nb):
     np.testing.assert_allclose(s2, o2, rtol=RTOL, atol=1e-13)
 
 
+def test_entropy2d_large_bins_explicit_pairs_vs_oracle(gpu, orc):
+    """More than 214 bins with an explicit pair list (ML, MM): histograms that
+    do not fit shared memory are counted in global memory."""
+    rng = np.random.default_rng(240)
+    ndof, nframes, nb = 6, 3001, 240
+    bins = (rng.integers(0, 40, size=(ndof, 1, nframes)) * 6 % nb).astype(np.uint8)
+    types = np.array([1, 1, 2, 2, 3, 3], np.uint8)
+    ext = np.tile(np.array([[0.5, 2.5, 1.5, 0.0]]), (ndof, 1))
+    ext[types == 3, 1] = 2 * np.pi
+    ext[types == 2, 1] = np.pi
+    pairs = np.array([(0, 5), (4, 1), (2, 3), (3, 2), (1, 2)], np.uint32)
+    p = make_params(nframes, 3, [nb], [0, 1], True)
+    s2 = gpu.entropy2d(p, types, bins, ext, pairs=pairs)
+    o2 = orc.entropy2d(pairs, types, bins, ext, 3, [nb], [0, 1], True)
+    np.testing.assert_allclose(s2, o2, rtol=RTOL, atol=1e-13)
+
+
 def test_entropy2d_rejects_bad_bins(gpu):
     bins = np.zeros((3, 1, 1000), np.uint8)
     bins[1, 0, 10] = 40
