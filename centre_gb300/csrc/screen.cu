@@ -259,31 +259,39 @@ mlp_fwd_bwd_kernel(const float *__restrict__ wbf, const float *__restrict__ X,
 //   block k < 64      : row k of W2 (lane m = t & 63) and b2[k]
 //   block 64 + m      : row m of W1 (lane q = t & 15, q < 12) and b1[m]
 //   block 128         : W3 (lane k = t & 63) and b3
+// Blocks along y take disjoint sample ranges and write their own partial
+// gradient rows (grad + y * kNParams); reduce_grad_kernel or the Adam kernel
+// sums the rows in a fixed order.
+constexpr int kGradSplit = 8;
+
 __global__ void __launch_bounds__(256)
 mlp_grad_kernel(const float *__restrict__ xs, const float *__restrict__ h1s,
                 const float *__restrict__ h2s, const float *__restrict__ dh1s,
                 const float *__restrict__ dh2s, const float *__restrict__ douts, uint32_t B,
-                float *__restrict__ grad) {
+                float *__restrict__ gradpart) {
   __shared__ float pw[256], pb[256];
   const int b = blockIdx.x, t = threadIdx.x;
+  const uint32_t per = (B + gridDim.y - 1) / gridDim.y;
+  const uint32_t sb = blockIdx.y * per, se = min(B, sb + per);
+  float *grad = gradpart + (uint64_t)blockIdx.y * kNParams;
   float aw = 0.f, ab = 0.f;
   if (b < kHid) {
     const int m = t & 63, part = t >> 6;
-    for (uint32_t s = part; s < B; s += 4) {
+    for (uint32_t s = sb + part; s < se; s += 4) {
       const float d = dh2s[(uint64_t)s * kHid + b];
       aw = fmaf(d, h1s[(uint64_t)s * kHid + m], aw);
       ab += d;
     }
   } else if (b < 2 * kHid) {
     const int m = b - kHid, q = t & 15, part = t >> 4;
-    for (uint32_t s = part; s < B; s += 16) {
+    for (uint32_t s = sb + part; s < se; s += 16) {
       const float d = dh1s[(uint64_t)s * kHid + m];
       if (q < kFeat) aw = fmaf(d, xs[(uint64_t)s * kFeat + q], aw);
       ab += d;
     }
   } else {
     const int k = t & 63, part = t >> 6;
-    for (uint32_t s = part; s < B; s += 4) {
+    for (uint32_t s = sb + part; s < se; s += 4) {
       const float d = douts[s];
       aw = fmaf(d, h2s[(uint64_t)s * kHid + k], aw);
       ab += d;
@@ -318,14 +326,24 @@ mlp_grad_kernel(const float *__restrict__ xs, const float *__restrict__ h1s,
 }
 
 // Adam on the FP32 master weights; the bf16-rounded copy feeds the kernels.
+__global__ void reduce_grad_kernel(const float *__restrict__ gradpart, float *__restrict__ g) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= kNParams) return;
+  float v = 0.f;
+  for (int k = 0; k < kGradSplit; ++k) v += gradpart[(uint64_t)k * kNParams + q];
+  g[q] = v;
+}
+
 __global__ void adam_kernel(float *__restrict__ w, float *__restrict__ wbf,
-                            const float *__restrict__ g, float *__restrict__ m1,
+                            const float *__restrict__ gradpart, float *__restrict__ m1,
                             float *__restrict__ m2, float lr, float c1, float c2) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= kNParams) return;
+  float gq = 0.f;
+  for (int k = 0; k < kGradSplit; ++k) gq += gradpart[(uint64_t)k * kNParams + q];
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-  m1[q] = b1 * m1[q] + (1.f - b1) * g[q];
-  m2[q] = b2 * m2[q] + (1.f - b2) * g[q] * g[q];
+  m1[q] = b1 * m1[q] + (1.f - b1) * gq;
+  m2[q] = b2 * m2[q] + (1.f - b2) * gq * gq;
   w[q] -= lr * (m1[q] / c1) / (sqrtf(m2[q] / c2) + eps);
   wbf[q] = bf16r(w[q]);
 }
@@ -580,10 +598,13 @@ extern "C" int centre_gpu_screen_mlp_grad(centre_ctx *ctx, const float *weights,
   mlp_fwd_bwd_kernel<<<(B + 127) / 128, 128, 0, st>>>(
       (float *)wbf.p, (float *)X.p, (float *)y.p, nullptr, 0, B, (float *)xs.p, (float *)h1.p,
       (float *)h2.p, (float *)dh1.p, (float *)dh2.p, (float *)dout.p, (float *)pr.p, (double *)ls.p);
-  mlp_grad_kernel<<<2 * kHid + 1, 256, 0, st>>>((float *)xs.p, (float *)h1.p, (float *)h2.p,
-                                                 (float *)dh1.p, (float *)dh2.p, (float *)dout.p,
-                                                 B, (float *)g.p);
-  ctx->launches += 3;
+  Buf gp;
+  CENTRE_TRY(dalloc(ctx, gp, sizeof(float) * kNParams * kGradSplit));
+  mlp_grad_kernel<<<dim3(2 * kHid + 1, kGradSplit), 256, 0, st>>>(
+      (float *)xs.p, (float *)h1.p, (float *)h2.p, (float *)dh1.p, (float *)dh2.p,
+      (float *)dout.p, B, (float *)gp.p);
+  reduce_grad_kernel<<<(kNParams + 255) / 256, 256, 0, st>>>((float *)gp.p, (float *)g.p);
+  ctx->launches += 4;
   CENTRE_CUDA(ctx, cudaGetLastError());
   double l = 0;
   CENTRE_CUDA(ctx, cudaMemcpyAsync(grad, g.p, sizeof(float) * kNParams, cudaMemcpyDeviceToHost, st));
@@ -693,7 +714,7 @@ extern "C" int centre_gpu_screen_dev(centre_ctx *ctx, const centre_entropy_param
     CENTRE_TRY(dalloc(ctx, dout, sizeof(float) * (size_t)B));
     CENTRE_TRY(dalloc(ctx, m1, sizeof(float) * kNParams));
     CENTRE_TRY(dalloc(ctx, m2, sizeof(float) * kNParams));
-    CENTRE_TRY(dalloc(ctx, g, sizeof(float) * kNParams));
+    CENTRE_TRY(dalloc(ctx, g, sizeof(float) * kNParams * kGradSplit));
     CENTRE_TRY(dalloc(ctx, ls, sizeof(double) * std::max<uint32_t>(sp->epochs, 1)));
     uint64_t s = sp->seed;
     std::vector<uint32_t> hp(2 * n);
@@ -731,10 +752,9 @@ extern "C" int centre_gpu_screen_dev(centre_ctx *ctx, const centre_entropy_param
             (float *)wbf.p, (float *)tX.p, (float *)ty.p, (uint32_t *)ord.p, q * B, B,
             (float *)xs.p, (float *)h1.p, (float *)h2.p, (float *)dh1.p, (float *)dh2.p,
             (float *)dout.p, nullptr, (double *)ls.p + ep);
-        mlp_grad_kernel<<<2 * kHid + 1, 256, 0, st>>>((float *)xs.p, (float *)h1.p,
-                                                       (float *)h2.p, (float *)dh1.p,
-                                                       (float *)dh2.p, (float *)dout.p, B,
-                                                       (float *)g.p);
+        mlp_grad_kernel<<<dim3(2 * kHid + 1, kGradSplit), 256, 0, st>>>(
+            (float *)xs.p, (float *)h1.p, (float *)h2.p, (float *)dh1.p, (float *)dh2.p,
+            (float *)dout.p, B, (float *)g.p);
         const float c1 = 1.f - powf(0.9f, (float)t), c2 = 1.f - powf(0.999f, (float)t);
         adam_kernel<<<(kNParams + 255) / 256, 256, 0, st>>>((float *)w.p, (float *)wbf.p,
                                                             (float *)g.p, (float *)m1.p,
