@@ -15,26 +15,31 @@
 //
 // Operand tiles stay zero in shared memory; producer warps write one E4M3 1.0
 // byte per (frame, DOF) into the K-major, 128-byte-swizzled tiles and clear
-// exactly those bytes again once the MMA has consumed the stage, so building
-// a one-hot tile costs two byte stores per (frame, DOF) instead of writing
-// the whole tile.  Lane l of a producer warp owns frames 4l..4l+3 of the
-// chunk for every DOF of the tile: its bins arrive in one coalesced 32-bit
-// load per DOF, and the stores of one instruction spread over all 32 banks.
+// exactly those bytes again (at addresses kept in registers) once the MMA has
+// consumed the stage, so building a one-hot tile costs two byte stores per
+// (frame, DOF) instead of writing the whole tile.  Lane l of a producer warp
+// owns frames 4l..4l+3 of the chunk: its bins arrive in one coalesced 32-bit
+// load per DOF, and the stores of one instruction spread over the banks.
 //
 // Convergence steps are prefixes of the frame axis: K-chunks never straddle a
-// step boundary, and at each boundary the epilogue warps read the running
-// accumulator from TMEM (tcgen05.ld), reduce each (row DOF, column DOF) block
-// to sum c ln c (exact 128-bit fixed point) and the non-empty cell count, and
-// add them into the pair's moments with integer atomics (tiles split pair
+// step boundary.  The MMAs of a step accumulate into TMEM columns [256, 512)
+// starting from zero; at the step's end the epilogue warps add them to the
+// cumulative counts in columns [0, 256) and release the accumulator at once,
+// so the next step's MMAs overlap the rest of the epilogue: reading the
+// cumulative counts (tcgen05.ld), reducing each (row DOF, column DOF) block to
+// sum c ln c (exact 128-bit fixed point) and the non-empty cell count, and
+// adding them into the pair's moments with integer atomics (tiles split pair
 // blocks; integer addition keeps the result independent of the split).
 //
-// Warp roles (288 threads): warp 0 allocates TMEM and one lane issues the
-// MMAs; warps 1-4 produce operand stages, warp 1+p owning stage p, so four
-// stages are built concurrently without cross-warp barriers, each warp
-// prefetching the bins of its next chunk into registers while it marks the
-// current one; warps 5-8 run the epilogue (TMEM lane group = warp % 4).  Every
-// mbarrier wait is bounded: on expiry the kernel sets an error flag, lets the
-// MMAs it issued drain (again bounded), frees its TMEM and returns.
+// Warp roles (544 threads): warp 0 allocates TMEM and one lane issues the
+// MMAs; warps 1-12 produce operand stages, three per stage (warp 1+p+4h marks
+// the DOF slots h, h+3, ... of stage p), so the four stages are built
+// concurrently without cross-warp barriers, each warp prefetching the bins of
+// its next chunk into registers while it marks the current one (the marking
+// is bound by instruction issue and latency; more warps hide it); warps 13-16
+// run the epilogue (TMEM lane group = warp % 4).  Every mbarrier wait is
+// bounded: on expiry the kernel sets an error flag, lets the MMAs it issued
+// drain (again bounded), frees its TMEM and returns.
 #include <algorithm>
 #include <vector>
 
@@ -56,11 +61,22 @@ constexpr int kMaxSlotsA = kTileM / kMinBins + 1;  // 9
 constexpr int kMaxSlotsB = kTileN / kMinBins + 1;  // 17
 constexpr int kMaxSlots = kMaxSlotsA + kMaxSlotsB;
 constexpr int kTabTc = 2048;                // c ln c doubles in shared memory
-constexpr int kProducerWarps = kStages;     // producer warp p owns stage p
+#ifndef CENTRE_TC_PRODUCERS_PER_STAGE
+#define CENTRE_TC_PRODUCERS_PER_STAGE 3
+#endif
+// Producer warps p, p + kStages, ... fill stage p, each the DOF slots
+// congruent to its rank modulo kPerStage (the marking is issue-bound: more
+// warps hide its latency).
+constexpr int kPerStage = CENTRE_TC_PRODUCERS_PER_STAGE;
+constexpr int kProducerWarps = kStages * kPerStage;
+constexpr int kSlotsPerWarp = (kMaxSlots + kPerStage - 1) / kPerStage;
 constexpr int kEpilogue = 128;
-constexpr int kThreads = 32 * (1 + kProducerWarps + 4);   // 288
+constexpr int kThreads = 32 * (1 + kProducerWarps + 4);   // 544 at three per stage
 constexpr int kFramesPerLane = kChunk / 32;              // 4
-constexpr unsigned kTmemCols = 256;
+// TMEM columns: [0, 256) the cumulative counts of the current step, read by
+// the epilogue; [256, 512) the MMA accumulator of the step's own frames
+constexpr unsigned kTmemCols = 512;
+constexpr uint32_t kIncCol = 256;
 constexpr long long kWaitCycles = 20000000000ll;  // ~10 s at 2 GHz
 constexpr uint8_t kOne = 0x38;              // 1.0 in E4M3
 
@@ -95,7 +111,14 @@ struct Smem {
   uint32_t tmem_base;
   int abort_flag;
   int ego[2];       // epilogue's per-snapshot go/abort decision
+  uint32_t sink;    // target of one-hot stores that fall outside a tile
   double tab[kTabTc];
+  // per (row DOF slot, column DOF slot) block of the tile: sum of c ln c as
+  // high part (bits 48+) and low 48 bits, both plain 64-bit sums, and the
+  // non-empty cell count; filled with shared-memory reductions
+  unsigned long long blk_lo[kMaxSlotsA * kMaxSlotsB];
+  unsigned long long blk_hi[kMaxSlotsA * kMaxSlotsB];
+  unsigned blk_nz[kMaxSlotsA * kMaxSlotsB];
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -109,14 +132,22 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
+  // the waiting thread may be suspended up to the hint (ns) instead of
+  // spinning, which leaves the issue slots to the warps doing work
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}\n"
       : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(20000u)
       : "memory");
   return ok != 0;
+}
+__device__ __forceinline__ void red_shared_u64(uint32_t addr, unsigned long long v) {
+  asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_shared_u32(uint32_t addr, unsigned v) {
+  asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
 }
 // Bounded wait: false when the kernel is aborting (timeout here or elsewhere).
 __device__ bool wait_bar(Smem &S, uint64_t *bar, uint32_t parity, int *flag) {
@@ -170,15 +201,46 @@ __device__ __forceinline__ void mma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t
       "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
       : "memory");
 }
+// 16 consecutive TMEM columns of the warp's 32 lanes (one row per thread)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+      "%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+      "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+      "r"(v[15])
+      : "memory");
+}
+// Wait for the thread's TMEM loads; the registers are operands so that no
+// use of them is scheduled before the wait.
+__device__ __forceinline__ void tmem_wait_ld16(uint32_t (&v)[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]),
+                 "+r"(v[6]), "+r"(v[7]), "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]),
+                 "+r"(v[12]), "+r"(v[13]), "+r"(v[14]), "+r"(v[15])
+               :
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld8(uint32_t (&v)[8]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]),
+                 "+r"(v[6]), "+r"(v[7])
+               :
+               : "memory");
+}
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
-}
-
-// Byte offset of element (row, k) in a K-major 128B-swizzled tile.
-__device__ __forceinline__ uint32_t swz(uint32_t row, uint32_t k) {
-  return (row >> 3) * 1024u + (row & 7u) * 128u + ((((k >> 4) ^ row) & 7u) << 4) + (k & 15u);
 }
 
 struct ChunkIter {
@@ -266,13 +328,15 @@ __device__ __forceinline__ void slot_info(const TcParams &P, const StageMeta &m,
 // registers.  The values are first used one chunk later (prefetch); the
 // range check happens when they are marked.
 __device__ __forceinline__ void load_lane_bins(const TcParams &P, const StageMeta &m, uint64_t f0,
-                                               int lane, uint32_t (&pb)[kMaxSlots], int *flag) {
+                                               int lane, int h, uint32_t (&pb)[kSlotsPerWarp],
+                                               int *flag) {
   const int nslots = m.nda + m.ndb;
   const uint64_t n = P.nframes;
   const int k0 = kFramesPerLane * lane;
   const int avail = max(0, min(kFramesPerLane, m.nvalid - k0));
 #pragma unroll
-  for (int slot = 0; slot < kMaxSlots; ++slot) {
+  for (int i = 0; i < kSlotsPerWarp; ++i) {
+    const int slot = h + i * kPerStage;
     uint32_t w = 0;
     if (slot < nslots && avail > 0) {
       bool isA;
@@ -289,7 +353,7 @@ __device__ __forceinline__ void load_lane_bins(const TcParams &P, const StageMet
         }
       }
     }
-    pb[slot] = w;
+    pb[i] = w;
   }
 }
 
@@ -304,70 +368,55 @@ __device__ __forceinline__ void sts_u8(uint32_t addr, uint32_t v) {
   asm volatile("st.shared.u8 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
 }
 
-// Write val at the one-hot positions of the lane's frames.  In a K-major
-// 128B-swizzled tile, element (row, k) sits at
-//   (row << 7) + ((((k >> 4) ^ row) & 7) << 4) + (k & 15).
-__device__ __forceinline__ void mark_lane(const TcParams &P, const StageMeta &m, uint32_t stage_s,
-                                          int lane, uint32_t (&pb)[kMaxSlots], uint32_t val,
-                                          bool check, int *flag) {
+// Set the one-hot bytes (E4M3 1.0) of the lane's frames and remember their
+// addresses for clearing.  In a K-major 128B-swizzled tile, element (row, k)
+// sits at (row << 7) + ((((k >> 4) ^ row) & 7) << 4) + (k & 15).  Positions
+// outside the tile (first/last DOF of a tile cut by its edge, frames past
+// the chunk's end) go to a scratch byte instead, so that clearing is one
+// unconditional store per position.
+constexpr int kLaneMarks = kSlotsPerWarp * kFramesPerLane;
+
+__device__ __forceinline__ void mark_set(const TcParams &P, const StageMeta &m, uint32_t stage_s,
+                                         uint32_t sink, int lane, int h,
+                                         uint32_t (&pb)[kSlotsPerWarp],
+                                         uint32_t (&addr)[kLaneMarks], int *flag) {
   const int nslots = m.nda + m.ndb;
   const int k0 = kFramesPerLane * lane;
   const uint32_t g = (uint32_t)(k0 >> 4);
   const uint32_t q0 = (uint32_t)(k0 & 15);
   const int kv = m.nvalid - k0;
 #pragma unroll
-  for (int slot = 0; slot < kMaxSlots; ++slot) {
-    if (slot >= nslots) break;
-    bool isA;
-    int dof, base;
-    slot_info(P, m, slot, isA, dof, base);
-    const uint32_t rows = isA ? kTileM : kTileN;
-    const uint32_t T = stage_s + (isA ? 0u : (uint32_t)kABytes);
-    if (check && __vcmpgeu4(pb[slot], 0x01010101u * (uint32_t)P.nb)) {
-      // a bin >= nb: report it and keep every store inside the tile
-      atomicOr(flag, kFlagBinRange);
-      pb[slot] = 0;
-    }
+  for (int i = 0; i < kSlotsPerWarp; ++i) {
+    const int slot = h + i * kPerStage;
+    if (slot < nslots) {
+      bool isA;
+      int dof, base;
+      slot_info(P, m, slot, isA, dof, base);
+      const uint32_t rows = isA ? kTileM : kTileN;
+      const uint32_t T = stage_s + (isA ? 0u : (uint32_t)kABytes) + q0;
+      if (__vcmpgeu4(pb[i], 0x01010101u * (uint32_t)P.nb)) {
+        // a bin >= nb: report it and keep every store inside the tile
+        atomicOr(flag, kFlagBinRange);
+        pb[i] = 0;
+      }
 #pragma unroll
-    for (int q = 0; q < kFramesPerLane; ++q) {
-      if (q >= kv) break;
-      const uint32_t row = (uint32_t)(base + (int)((pb[slot] >> (8 * q)) & 255u));
-      if (row < rows) sts_u8(T + (row << 7) + (((g ^ row) & 7u) << 4) + q0 + q, val);
+      for (int q = 0; q < kFramesPerLane; ++q) {
+        const uint32_t row = (uint32_t)(base + (int)((pb[i] >> (8 * q)) & 255u));
+        const uint32_t a = T + (row << 7) + (((g ^ row) & 7u) << 4) + q;
+        addr[i * kFramesPerLane + q] = (row < rows && q < kv) ? a : sink;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < kFramesPerLane; ++q) addr[i * kFramesPerLane + q] = sink;
     }
   }
+#pragma unroll
+  for (int j = 0; j < kLaneMarks; ++j) sts_u8(addr[j], kOne);
 }
 
-// Add one row segment's (sum c ln c, non-empty cells) to pair (rd, cd): the
-// lanes of a warp hold consecutive rows, so rows of the same DOF are
-// contiguous lanes; a segmented shuffle reduction leaves each DOF's total in
-// its first lane, which adds it to the pair's moments.
-__device__ __noinline__ void flush_segment(const TcParams &P, U128 a, unsigned z, int rd,
-                                              bool rowvalid, int cd, int t, int lane,
-                                              U128 *__restrict__ sclnc,
-                                              unsigned *__restrict__ nnz) {
+__device__ __forceinline__ void mark_clear(const uint32_t (&addr)[kLaneMarks]) {
 #pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    U128 od;
-    od.lo = __shfl_down_sync(0xffffffffu, a.lo, off);
-    od.hi = __shfl_down_sync(0xffffffffu, a.hi, off);
-    const unsigned oz = __shfl_down_sync(0xffffffffu, z, off);
-    const int ord = __shfl_down_sync(0xffffffffu, rd, off);
-    if (lane + off < 32 && ord == rd) {
-      a = u128_add(a, od);
-      z += oz;
-    }
-  }
-  const int prd = __shfl_up_sync(0xffffffffu, rd, 1);
-  const bool head = (lane == 0) || (prd != rd);
-  if (head && rowvalid && rd < cd && cd < (int)P.ndof) {
-    const uint64_t pidx =
-        (uint64_t)rd * P.ndof - (uint64_t)rd * (rd + 1) / 2 + (uint64_t)(cd - rd - 1);
-    U128 *dst = sclnc + pidx * P.nsteps + t;
-    const unsigned long long old = atomicAdd(&dst->lo, a.lo);
-    const unsigned long long carry = (old + a.lo < old) ? 1ull : 0ull;
-    atomicAdd(&dst->hi, a.hi + carry);
-    atomicAdd(&nnz[pidx * P.nsteps + t], z);
-  }
+  for (int j = 0; j < kLaneMarks; ++j) sts_u8(addr[j], 0u);
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -387,10 +436,15 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
     uint4 *p = reinterpret_cast<uint4 *>(stages);
     for (int i = tid; i < kStages * kStageBytes / 16; i += kThreads) p[i] = z;
     for (int i = tid; i < kTabTc; i += kThreads) S.tab[i] = gtab[i];
+    for (int i = tid; i < kMaxSlotsA * kMaxSlotsB; i += kThreads) {
+      S.blk_lo[i] = 0ull;
+      S.blk_hi[i] = 0ull;
+      S.blk_nz[i] = 0u;
+    }
   }
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&S.full[s], 32);
+      mbar_init(&S.full[s], 32 * kPerStage);
       mbar_init(&S.empty[s], 1);
     }
     mbar_init(&S.accfull, 1);
@@ -416,7 +470,7 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
     // ---- MMA issuer --------------------------------------------------------
     if (lane == 0) {
       int s = 0;
-      uint32_t ph[kStages] = {0, 0, 0, 0};
+      uint32_t ph[kStages] = {};
       uint32_t nsnap = 0;
       bool issued = false;
       bool ok = true;
@@ -434,7 +488,7 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
           const uint32_t b0 = a0 + kABytes;
           const int nk = (int)((f1 - f0 + 31) / 32);
           for (int k = 0; k < nk; ++k) {
-            mma_f8(tmem, sw128_desc(a0 + 32u * k), sw128_desc(b0 + 32u * k),
+            mma_f8(tmem + kIncCol, sw128_desc(a0 + 32u * k), sw128_desc(b0 + 32u * k),
                    (first && k == 0) ? 0u : 1u);
           }
           issued = true;
@@ -444,9 +498,11 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
           if (last) {
             mma_commit(&S.accfull);
             ++nsnap;
-            // wait until the epilogue has read this snapshot
+            // wait until the epilogue has added this step's counts to the
+            // cumulative ones; the next step starts from zero
             if (!wait_bar(S, &S.accempty, (nsnap - 1) & 1u, flag)) { ok = false; break; }
             tc_fence_after();
+            first = true;
           }
         }
       }
@@ -464,14 +520,16 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
     }
     __syncwarp();
   } else if (warp <= kProducerWarps) {
-    // ---- producers: warp 1+p builds every chunk c with c % 4 == p ------------
-    const int p = warp - 1;
+    // ---- producers: warps 1+p, 1+p+kStages, ... build every chunk c with
+    // c % kStages == p, warp rank h marking the DOF slots h, h+kPerStage, ...
+    const int p = (warp - 1) % kStages;
+    const int h = (warp - 1) / kStages;
     const uint32_t stage_s = stages_s + (uint32_t)(p * kStageBytes);
     uint32_t ph = 0;
     bool used = false;
-    StageMeta old;            // previous occupant of this stage
-    uint32_t oldb[kMaxSlots];
-    uint32_t pb[kMaxSlots];
+    const uint32_t sink = smem_u32(&S.sink);
+    uint32_t addr[kLaneMarks];   // one-hot positions set for the stage's occupant
+    uint32_t pb[kSlotsPerWarp];
     ChunkWalker walk;
     walk.start(blockIdx.x, gridDim.x, P.ntiles, P.step_size, P.nsteps);
     ChunkPos cur;
@@ -480,7 +538,7 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
     if (cur.valid) {
       tile_geometry(P, P.tiles[cur.ti], m);
       m.nvalid = (int)(cur.f1 - cur.f0);
-      load_lane_bins(P, m, cur.f0, lane, pb, flag);
+      load_lane_bins(P, m, cur.f0, lane, h, pb, flag);
     }
     while (cur.valid) {
       // wait until the MMA has consumed this stage's previous chunk
@@ -490,22 +548,19 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
       if (!go) break;
       if (used) {
         ph ^= 1u;
-        mark_lane(P, old, stage_s, lane, oldb, 0u, false, flag);
+        mark_clear(addr);
       }
       __syncwarp();
-      mark_lane(P, m, stage_s, lane, pb, kOne, true, flag);
+      mark_set(P, m, stage_s, sink, lane, h, pb, addr, flag);
       fence_proxy_async();
       mbar_arrive(&S.full[p]);
-      // remember what was set, then fetch this warp's next chunk
-      old = m;
-#pragma unroll
-      for (int i = 0; i < kMaxSlots; ++i) oldb[i] = pb[i];
+      // fetch this warp's next chunk
       used = true;
-      for (int i = 0; i < kProducerWarps; ++i) cur = walk.next();
+      for (int i = 0; i < kStages; ++i) cur = walk.next();
       if (cur.valid) {
         tile_geometry(P, P.tiles[cur.ti], m);
         m.nvalid = (int)(cur.f1 - cur.f0);
-        load_lane_bins(P, m, cur.f0, lane, pb, flag);
+        load_lane_bins(P, m, cur.f0, lane, h, pb, flag);
       }
     }
   } else {
@@ -530,48 +585,102 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
         named_bar(2, kEpilogue);
         if (!*(volatile int *)&S.ego[nsnap & 1u]) { ok = false; break; }
         tc_fence_after();
+        const uint32_t trow = tmem + ((uint32_t)(32 * ew) << 16);
+        // Add the step's counts to the cumulative ones (the first step of a
+        // tile replaces them) and release the MMA accumulator at once.
+#pragma unroll 1
+        for (int c = 0; c < kTileN; c += 16) {
+          uint32_t inc[16], cum[16];
+          tmem_ld16(trow + kIncCol + (uint32_t)c, inc);
+          if (t > 0) {
+            tmem_ld16(trow + (uint32_t)c, cum);
+            tmem_wait_ld16(cum);
+          }
+          tmem_wait_ld16(inc);
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            cum[j] = (t > 0) ? __float_as_uint(__uint_as_float(inc[j]) + __uint_as_float(cum[j]))
+                             : inc[j];
+          tmem_st16(trow + (uint32_t)c, cum);
+        }
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        tc_fence_before();
+        mbar_arrive(&S.accempty);
+        // Each thread reads its accumulator row in chunks of 8 columns,
+        // sums the exact c ln c of its cells per column DOF in registers
+        // and adds each row segment to the tile's (row DOF, column DOF)
+        // block in shared memory.  Once the last chunk is read, the MMA may
+        // continue; the blocks are then added to their pairs' moments, one
+        // thread per block.
+        const int rs = rowvalid ? rd - m.d0a : -1;     // row DOF slot
         U128 acc;
         acc.lo = acc.hi = 0ull;
         unsigned cnz = 0;
-        int cur = m.cb / nb;                       // column DOF of column 0
-        int nextb = (cur + 1) * nb - m.cb;         // first column of the next DOF
-        for (int chunk = 0; chunk < kTileN / 32; ++chunk) {
-          uint32_t v[32];
-          const uint32_t taddr = tmem + ((uint32_t)(32 * ew) << 16) + (uint32_t)(chunk * 32);
+        int cs = 0;                                    // column DOF slot
+        int nextb = (m.d0b + 1) * nb - m.cb;           // first column of the next DOF
+        auto flush = [&]() {
+          if (rs >= 0 && cnz) {
+            const uint32_t bi = (uint32_t)(rs * kMaxSlotsB + cs);
+            red_shared_u64(smem_u32(&S.blk_lo[bi]), acc.lo & 0xFFFFFFFFFFFFull);
+            red_shared_u64(smem_u32(&S.blk_hi[bi]), (acc.lo >> 48) | (acc.hi << 16));
+            red_shared_u32(smem_u32(&S.blk_nz[bi]), cnz);
+          }
+          acc.lo = acc.hi = 0ull;
+          cnz = 0;
+        };
+#pragma unroll 1
+        for (int chunk = 0; chunk < kTileN / 8; ++chunk) {
+          uint32_t v[8];
+          const uint32_t taddr = trow + (uint32_t)(chunk * 8);
           asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-              "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-              "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+              "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-                "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
-                "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-                "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
-                "=r"(v[30]), "=r"(v[31])
+                "=r"(v[6]), "=r"(v[7])
               : "r"(taddr));
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          tmem_wait_ld8(v);
+          unsigned cnt[8];
+          double dv[8];
 #pragma unroll
-          for (int q = 0; q < 32; ++q) {
-            const int c = chunk * 32 + q;
-            if (c == nextb) {
-              flush_segment(P, acc, cnz, rd, rowvalid, cur, t, lane, sclnc, nnz);
-              acc.lo = acc.hi = 0ull;
-              cnz = 0;
-              ++cur;
+          for (int q = 0; q < 8; ++q) {
+            // exact integer count from the FP32 accumulator
+            cnt[q] = __float_as_uint(__uint_as_float(v[q]) + 8388608.0f) - 0x4B000000u;
+            dv[q] = (cnt[q] < (unsigned)kTabTc) ? S.tab[cnt[q]] : clnc_far(gtab, cnt[q]);
+          }
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            if (chunk * 8 + q == nextb) {
+              flush();
+              ++cs;
               nextb += nb;
             }
-            // exact integer count from the FP32 accumulator
-            const unsigned cnt = __float_as_uint(__uint_as_float(v[q]) + 8388608.0f) - 0x4B000000u;
-            if (cnt) {
-              const double dv = (cnt < (unsigned)kTabTc) ? S.tab[cnt] : clnc_far(gtab, cnt);
-              acc = u128_add(acc, u128_from_double(dv));
-              ++cnz;
-            }
+            acc = u128_add(acc, u128_from_double(dv[q]));
+            cnz += (cnt[q] != 0u);
           }
         }
-        flush_segment(P, acc, cnz, rd, rowvalid, cur, t, lane, sclnc, nnz);
-        tc_fence_before();
-        mbar_arrive(&S.accempty);
+        flush();
+        named_bar(2, kEpilogue);
+        for (int i = etid; i < kMaxSlotsA * kMaxSlotsB; i += kEpilogue) {
+          const unsigned z = S.blk_nz[i];
+          if (z) {
+            const int rdb = m.d0a + i / kMaxSlotsB, cdb = m.d0b + i % kMaxSlotsB;
+            if (rdb < cdb && cdb < (int)P.ndof) {
+              const unsigned long long lo = S.blk_lo[i], hi = S.blk_hi[i];
+              U128 tot;
+              tot.lo = lo + (hi << 48);
+              tot.hi = (hi >> 16) + ((tot.lo < lo) ? 1ull : 0ull);
+              const uint64_t pidx = (uint64_t)rdb * P.ndof - (uint64_t)rdb * (rdb + 1) / 2 +
+                                    (uint64_t)(cdb - rdb - 1);
+              U128 *dst = sclnc + pidx * P.nsteps + t;
+              const unsigned long long old = atomicAdd(&dst->lo, tot.lo);
+              const unsigned long long carry = (old + tot.lo < old) ? 1ull : 0ull;
+              atomicAdd(&dst->hi, tot.hi + carry);
+              atomicAdd(&nnz[pidx * P.nsteps + t], z);
+            }
+          }
+          S.blk_lo[i] = 0ull;
+          S.blk_hi[i] = 0ull;
+          S.blk_nz[i] = 0u;
+        }
         ++nsnap;
       }
     }
