@@ -105,8 +105,9 @@ __device__ __forceinline__ U128 u128_from_double(double v) {
   U128 r;
   r.lo = 0ull;
   r.hi = 0ull;
-  if (v == 0.0) return r;
+  // integer test for +-0 (no FP64 instruction: FP64 issue is scarce on this part)
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  if ((bits << 1) == 0ull) return r;
   const int s = (int)((bits >> 52) & 0x7ff) - 1023 + 8;  // value = m * 2^(e - 52 + 60)
   const unsigned long long m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
   if (s >= 64) {

@@ -60,7 +60,7 @@ constexpr int kMinBins = 16;                // DOF slots per tile bounded below
 constexpr int kMaxSlotsA = kTileM / kMinBins + 1;  // 9
 constexpr int kMaxSlotsB = kTileN / kMinBins + 1;  // 17
 constexpr int kMaxSlots = kMaxSlotsA + kMaxSlotsB;
-constexpr int kTabTc = 2048;                // c ln c doubles in shared memory
+constexpr int kTabTc = 1024;                // 128-bit c ln c entries in shared memory
 #ifndef CENTRE_TC_PRODUCERS_PER_STAGE
 #define CENTRE_TC_PRODUCERS_PER_STAGE 3
 #endif
@@ -70,8 +70,16 @@ constexpr int kTabTc = 2048;                // c ln c doubles in shared memory
 constexpr int kPerStage = CENTRE_TC_PRODUCERS_PER_STAGE;
 constexpr int kProducerWarps = kStages * kPerStage;
 constexpr int kSlotsPerWarp = (kMaxSlots + kPerStage - 1) / kPerStage;
-constexpr int kEpilogue = 128;
-constexpr int kThreads = 32 * (1 + kProducerWarps + 4);   // 544 at three per stage
+// Epilogue: kEpiGroups warp quartets, quartet g reading accumulator columns
+// [g * kEpiCols, (g + 1) * kEpiCols) of all 128 rows (a warp reads the TMEM
+// lanes of its warp index modulo 4).
+#ifndef CENTRE_TC_EPI_GROUPS
+#define CENTRE_TC_EPI_GROUPS 2
+#endif
+constexpr int kEpiGroups = CENTRE_TC_EPI_GROUPS;
+constexpr int kEpiCols = kTileN / kEpiGroups;
+constexpr int kEpilogue = 128 * kEpiGroups;
+constexpr int kThreads = 32 * (1 + kProducerWarps + 4 * kEpiGroups);
 constexpr int kFramesPerLane = kChunk / 32;              // 4
 // TMEM columns: [0, 256) the cumulative counts of the current step, read by
 // the epilogue; [256, 512) the MMA accumulator of the step's own frames
@@ -102,6 +110,18 @@ struct StageMeta {
   int used;
 };
 
+// A producer warp's DOF slot of the current tile: the DOF's bins row
+// (element offset), the stage address of the slot's row 0 (tile row
+// `base` = row of the DOF's bin 0 relative to the tile, may be negative), and
+// the tile's row count.
+struct SlotInfo {
+  uint64_t src;
+  uint32_t tb;
+  int base;
+  int rows;
+  int pad;
+};
+
 struct Smem {
   uint64_t full[kStages];
   uint64_t empty[kStages];
@@ -112,7 +132,9 @@ struct Smem {
   int abort_flag;
   int ego[2];       // epilogue's per-snapshot go/abort decision
   uint32_t sink;    // target of one-hot stores that fall outside a tile
-  double tab[kTabTc];
+  // per producer warp, its DOF slots of the current tile (see SlotInfo)
+  SlotInfo slots[kProducerWarps][kSlotsPerWarp];
+  __align__(16) U128 tab[kTabTc];   // c ln c as 128-bit fixed point
   // per (row DOF slot, column DOF slot) block of the tile: sum of c ln c as
   // high part (bits 48+) and low 48 bits, both plain 64-bit sums, and the
   // non-empty cell count; filled with shared-memory reductions
@@ -230,10 +252,16 @@ __device__ __forceinline__ void tmem_wait_ld16(uint32_t (&v)[16]) {
                :
                : "memory");
 }
-__device__ __forceinline__ void tmem_wait_ld8(uint32_t (&v)[8]) {
+// The epilogue's column chunk: kEpiW columns of the warp's 32 lanes.
+constexpr int kEpiW = 4;
+__device__ __forceinline__ void tmem_ld_w(uint32_t taddr, uint32_t (&v)[kEpiW]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3])
+               : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld_w(uint32_t (&v)[kEpiW]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;"
-               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]),
-                 "+r"(v[6]), "+r"(v[7])
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3])
                :
                : "memory");
 }
@@ -248,22 +276,26 @@ struct ChunkIter {
   uint64_t ss;
   int nsteps;
   int t;
-  uint64_t f;   // next frame
+  uint64_t f;     // next frame
+  uint64_t end;   // end of step t
   __device__ void start(uint64_t step_size, int ns) {
     ss = step_size;
     nsteps = ns;
     t = 0;
     f = 0;
+    end = step_size;
   }
   // returns false when done; sets [f0, f1) and whether it closes a step
   __device__ bool next(uint64_t &f0, uint64_t &f1, bool &last_of_step) {
     if (t >= nsteps) return false;
-    const uint64_t end = (uint64_t)(t + 1) * ss;
     f0 = f;
     f1 = min(end, f0 + (uint64_t)kChunk);
     last_of_step = (f1 == end);
     f = f1;
-    if (last_of_step) ++t;
+    if (last_of_step) {
+      ++t;
+      end += ss;
+    }
     return true;
   }
 };
@@ -324,44 +356,33 @@ __device__ __forceinline__ void slot_info(const TcParams &P, const StageMeta &m,
   base = dof * P.nb - (isA ? m.rb : m.cb);
 }
 
-// Load lane's 4 frames (4*lane .. +3 of the chunk) of every DOF slot into
-// registers.  The values are first used one chunk later (prefetch); the
-// range check happens when they are marked.
-__device__ __forceinline__ void load_lane_bins(const TcParams &P, const StageMeta &m, uint64_t f0,
-                                               int lane, int h, uint32_t (&pb)[kSlotsPerWarp],
-                                               int *flag) {
-  const int nslots = m.nda + m.ndb;
-  const uint64_t n = P.nframes;
+// c ln c for counts beyond the global table (rare), as 128-bit fixed point.
+// Kept out of line so the unrolled epilogue loop stays small.
+__device__ __noinline__ U128 clnc_far(unsigned c) { return clnc_fixed(c); }
+
+// Load the lane's 4 frames (4*lane .. +3 of the chunk) of the warp's DOF
+// slots into registers.  The values are first used one chunk later
+// (prefetch); the range check happens when they are marked.
+__device__ __forceinline__ void load_lane_bins(const TcParams &P, const SlotInfo *sl, int nmine,
+                                               int nvalid, uint64_t f0, int lane,
+                                               uint32_t (&pb)[kSlotsPerWarp]) {
   const int k0 = kFramesPerLane * lane;
-  const int avail = max(0, min(kFramesPerLane, m.nvalid - k0));
+  const int avail = max(0, min(kFramesPerLane, nvalid - k0));
 #pragma unroll
   for (int i = 0; i < kSlotsPerWarp; ++i) {
-    const int slot = h + i * kPerStage;
     uint32_t w = 0;
-    if (slot < nslots && avail > 0) {
-      bool isA;
-      int dof, base;
-      slot_info(P, m, slot, isA, dof, base);
-      if (dof < (int)P.ndof) {
-        const uint8_t *src = P.bins + ((uint64_t)dof * P.nschemes + P.scheme) * n + f0 + k0;
-        if (avail == kFramesPerLane && ((reinterpret_cast<uintptr_t>(src) & 3u) == 0)) {
-          w = __ldg(reinterpret_cast<const uint32_t *>(src));
-        } else {
+    if (i < nmine && avail > 0) {
+      const uint8_t *src = P.bins + sl[i].src + f0 + k0;
+      if (avail == kFramesPerLane && ((reinterpret_cast<uintptr_t>(src) & 3u) == 0)) {
+        w = __ldg(reinterpret_cast<const uint32_t *>(src));
+      } else {
 #pragma unroll
-          for (int q = 0; q < kFramesPerLane; ++q)
-            if (q < avail) w |= (uint32_t)__ldg(src + q) << (8 * q);
-        }
+        for (int q = 0; q < kFramesPerLane; ++q)
+          if (q < avail) w |= (uint32_t)__ldg(src + q) << (8 * q);
       }
     }
     pb[i] = w;
   }
-}
-
-// c ln c for counts beyond the shared-memory table (rare): the global table,
-// then the expression itself.  Kept out of line so the unrolled epilogue
-// loop stays small.
-__device__ __noinline__ double clnc_far(const double *__restrict__ gtab, unsigned c) {
-  return (c < (unsigned)kTabGlobal) ? __ldg(gtab + c) : clnc_value(c);
 }
 
 __device__ __forceinline__ void sts_u8(uint32_t addr, uint32_t v) {
@@ -373,37 +394,45 @@ __device__ __forceinline__ void sts_u8(uint32_t addr, uint32_t v) {
 // sits at (row << 7) + ((((k >> 4) ^ row) & 7) << 4) + (k & 15).  Positions
 // outside the tile (first/last DOF of a tile cut by its edge, frames past
 // the chunk's end) go to a scratch byte instead, so that clearing is one
-// unconditional store per position.
+// unconditional store per position.  Slots whose DOF lies inside the tile
+// take the path without those checks when the chunk is full.
 constexpr int kLaneMarks = kSlotsPerWarp * kFramesPerLane;
 
-__device__ __forceinline__ void mark_set(const TcParams &P, const StageMeta &m, uint32_t stage_s,
-                                         uint32_t sink, int lane, int h,
+__device__ __forceinline__ void mark_set(const TcParams &P, const SlotInfo *sl, int nmine,
+                                         uint32_t edgemask, int nvalid, uint32_t sink, int lane,
                                          uint32_t (&pb)[kSlotsPerWarp],
                                          uint32_t (&addr)[kLaneMarks], int *flag) {
-  const int nslots = m.nda + m.ndb;
   const int k0 = kFramesPerLane * lane;
   const uint32_t g = (uint32_t)(k0 >> 4);
   const uint32_t q0 = (uint32_t)(k0 & 15);
-  const int kv = m.nvalid - k0;
+  const int kv = nvalid - k0;
+  const bool full = nvalid == kChunk;
 #pragma unroll
   for (int i = 0; i < kSlotsPerWarp; ++i) {
-    const int slot = h + i * kPerStage;
-    if (slot < nslots) {
-      bool isA;
-      int dof, base;
-      slot_info(P, m, slot, isA, dof, base);
-      const uint32_t rows = isA ? kTileM : kTileN;
-      const uint32_t T = stage_s + (isA ? 0u : (uint32_t)kABytes) + q0;
+    if (i < nmine) {
+      const int base = sl[i].base;
+      const uint32_t tbq = sl[i].tb + q0;
       if (__vcmpgeu4(pb[i], 0x01010101u * (uint32_t)P.nb)) {
         // a bin >= nb: report it and keep every store inside the tile
         atomicOr(flag, kFlagBinRange);
         pb[i] = 0;
       }
+      if (full && !((edgemask >> i) & 1u)) {
 #pragma unroll
-      for (int q = 0; q < kFramesPerLane; ++q) {
-        const uint32_t row = (uint32_t)(base + (int)((pb[i] >> (8 * q)) & 255u));
-        const uint32_t a = T + (row << 7) + (((g ^ row) & 7u) << 4) + q;
-        addr[i * kFramesPerLane + q] = (row < rows && q < kv) ? a : sink;
+        for (int q = 0; q < kFramesPerLane; ++q) {
+          const uint32_t b = (pb[i] >> (8 * q)) & 255u;
+          const uint32_t row = (uint32_t)base + b;
+          addr[i * kFramesPerLane + q] = tbq + (b << 7) + (((g ^ row) & 7u) << 4) + q;
+        }
+      } else {
+        const uint32_t rows = (uint32_t)sl[i].rows;
+#pragma unroll
+        for (int q = 0; q < kFramesPerLane; ++q) {
+          const uint32_t b = (pb[i] >> (8 * q)) & 255u;
+          const uint32_t row = (uint32_t)base + b;
+          const uint32_t a = tbq + (b << 7) + (((g ^ row) & 7u) << 4) + q;
+          addr[i * kFramesPerLane + q] = (row < rows && q < kv) ? a : sink;
+        }
       }
     } else {
 #pragma unroll
@@ -435,7 +464,7 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
     uint4 z = make_uint4(0, 0, 0, 0);
     uint4 *p = reinterpret_cast<uint4 *>(stages);
     for (int i = tid; i < kStages * kStageBytes / 16; i += kThreads) p[i] = z;
-    for (int i = tid; i < kTabTc; i += kThreads) S.tab[i] = gtab[i];
+    for (int i = tid; i < kTabTc; i += kThreads) S.tab[i] = u128_from_double(gtab[i]);
     for (int i = tid; i < kMaxSlotsA * kMaxSlotsB; i += kThreads) {
       S.blk_lo[i] = 0ull;
       S.blk_hi[i] = 0ull;
@@ -528,17 +557,48 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
     uint32_t ph = 0;
     bool used = false;
     const uint32_t sink = smem_u32(&S.sink);
+    const int pw = warp - 1;
+    SlotInfo *sl = S.slots[pw];
     uint32_t addr[kLaneMarks];   // one-hot positions set for the stage's occupant
     uint32_t pb[kSlotsPerWarp];
     ChunkWalker walk;
     walk.start(blockIdx.x, gridDim.x, P.ntiles, P.step_size, P.nsteps);
     ChunkPos cur;
     for (int i = 0; i <= p; ++i) cur = walk.next();   // this warp's first chunk
-    StageMeta m;
+    uint64_t tile = ~0ull;       // tile whose slots are in sl[]
+    int nmine = 0;               // this warp's DOF slots in that tile
+    uint32_t edgemask = 0;       // slots whose DOF is cut by the tile's edge
+    // slot table of tile ti: lane i describes this warp's slot i
+    auto set_tile = [&](uint64_t ti) {
+      StageMeta m;
+      tile_geometry(P, P.tiles[ti], m);
+      const int slot = h + lane * kPerStage;
+      const bool valid = lane < kSlotsPerWarp && slot < m.nda + m.ndb;
+      bool edge = false;
+      if (valid) {
+        bool isA;
+        int dof, base;
+        slot_info(P, m, slot, isA, dof, base);
+        const int rows = isA ? kTileM : kTileN;
+        SlotInfo si;
+        si.src = ((uint64_t)dof * P.nschemes + P.scheme) * P.nframes;
+        si.tb = stage_s + (isA ? 0u : (uint32_t)kABytes) + ((uint32_t)base << 7);
+        si.base = base;
+        si.rows = rows;
+        si.pad = 0;
+        sl[lane] = si;
+        edge = base < 0 || base + P.nb > rows;
+      }
+      nmine = __popc(__ballot_sync(0xffffffffu, valid));
+      edgemask = __ballot_sync(0xffffffffu, edge);
+      tile = ti;
+      __syncwarp();
+    };
+    int nvalid = 0;
     if (cur.valid) {
-      tile_geometry(P, P.tiles[cur.ti], m);
-      m.nvalid = (int)(cur.f1 - cur.f0);
-      load_lane_bins(P, m, cur.f0, lane, h, pb, flag);
+      set_tile(cur.ti);
+      nvalid = (int)(cur.f1 - cur.f0);
+      load_lane_bins(P, sl, nmine, nvalid, cur.f0, lane, pb);
     }
     while (cur.valid) {
       // wait until the MMA has consumed this stage's previous chunk
@@ -551,22 +611,24 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
         mark_clear(addr);
       }
       __syncwarp();
-      mark_set(P, m, stage_s, sink, lane, h, pb, addr, flag);
+      mark_set(P, sl, nmine, edgemask, nvalid, sink, lane, pb, addr, flag);
       fence_proxy_async();
       mbar_arrive(&S.full[p]);
       // fetch this warp's next chunk
       used = true;
       for (int i = 0; i < kStages; ++i) cur = walk.next();
       if (cur.valid) {
-        tile_geometry(P, P.tiles[cur.ti], m);
-        m.nvalid = (int)(cur.f1 - cur.f0);
-        load_lane_bins(P, m, cur.f0, lane, h, pb, flag);
+        if (cur.ti != tile) set_tile(cur.ti);
+        nvalid = (int)(cur.f1 - cur.f0);
+        load_lane_bins(P, sl, nmine, nvalid, cur.f0, lane, pb);
       }
     }
   } else {
     // ---- epilogue ------------------------------------------------------------
     const int ew = warp & 3;             // TMEM lane group of this warp
     const int etid = 32 * ew + lane;     // accumulator row
+    const int eth = 32 * (warp - 1 - kProducerWarps) + lane;   // 0 .. kEpilogue-1
+    const int col0 = (eth / 128) * kEpiCols;                  // this quartet's columns
     uint32_t nsnap = 0;
     bool ok = true;
     const int nb = P.nb;
@@ -576,8 +638,13 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
       const int grow = m.rb + etid;
       const int rd = grow / nb;
       const bool rowvalid = grow < (int)P.nrows;
+      // this lane's row DOF segment within the warp: lanes [first, seg_end)
+      const int wrow0 = m.rb + 32 * ew;
+      const int seg_end = rowvalid ? min(32, (rd + 1) * nb - wrow0) : 32;
+      const bool seg_head = rowvalid && lane == max(0, rd * nb - wrow0);
+      const int seg_max = min(32, nb);       // longest segment (warp-uniform)
       for (int t = 0; t < P.nsteps; ++t) {
-        if (etid == 0) {
+        if (eth == 0) {
           bool go = wait_bar(S, &S.accfull, nsnap & 1u, flag);
           if (*(volatile int *)&S.abort_flag) go = false;
           S.ego[nsnap & 1u] = go ? 1 : 0;
@@ -589,7 +656,7 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
         // Add the step's counts to the cumulative ones (the first step of a
         // tile replaces them) and release the MMA accumulator at once.
 #pragma unroll 1
-        for (int c = 0; c < kTileN; c += 16) {
+        for (int c = col0; c < col0 + kEpiCols; c += 16) {
           uint32_t inc[16], cum[16];
           tmem_ld16(trow + kIncCol + (uint32_t)c, inc);
           if (t > 0) {
@@ -606,60 +673,109 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         tc_fence_before();
         mbar_arrive(&S.accempty);
-        // Each thread reads its accumulator row in chunks of 8 columns,
-        // sums the exact c ln c of its cells per column DOF in registers
-        // and adds each row segment to the tile's (row DOF, column DOF)
-        // block in shared memory.  Once the last chunk is read, the MMA may
-        // continue; the blocks are then added to their pairs' moments, one
-        // thread per block.
+        // Each thread reads its row of the cumulative counts in chunks of 8
+        // columns and sums the exact c ln c of its cells per column DOF in
+        // registers.  At each column DOF boundary the rows of one row DOF
+        // (consecutive lanes) are summed with a segmented warp reduction and
+        // the segment's first lane adds the sum to the tile's (row DOF,
+        // column DOF) block in shared memory (one atomic per warp segment:
+        // 64-bit shared-memory atomics on one address from many lanes
+        // serialise).  The blocks are then added to their pairs' moments,
+        // one thread per block.
         const int rs = rowvalid ? rd - m.d0a : -1;     // row DOF slot
         U128 acc;
         acc.lo = acc.hi = 0ull;
         unsigned cnz = 0;
-        int cs = 0;                                    // column DOF slot
-        int nextb = (m.d0b + 1) * nb - m.cb;           // first column of the next DOF
+        const int dcol = (m.cb + col0) / nb;           // DOF of the first column
+        int cs = dcol - m.d0b;                         // column DOF slot
+        int nextb = (dcol + 1) * nb - m.cb;            // first column of the next DOF
         auto flush = [&]() {
-          if (rs >= 0 && cnz) {
+          unsigned long long lo = acc.lo & 0xFFFFFFFFFFFFull;
+          unsigned long long hi = (acc.lo >> 48) | (acc.hi << 16);
+          unsigned z = cnz;
+#pragma unroll
+          for (int off = 1; off < 32; off <<= 1) {
+            if (off >= seg_max) break;
+            const unsigned long long lo2 = __shfl_down_sync(0xffffffffu, lo, off);
+            const unsigned long long hi2 = __shfl_down_sync(0xffffffffu, hi, off);
+            const unsigned z2 = __shfl_down_sync(0xffffffffu, z, off);
+            if (lane + off < seg_end) {
+              lo += lo2;
+              hi += hi2;
+              z += z2;
+            }
+          }
+          if (seg_head && z) {
             const uint32_t bi = (uint32_t)(rs * kMaxSlotsB + cs);
-            red_shared_u64(smem_u32(&S.blk_lo[bi]), acc.lo & 0xFFFFFFFFFFFFull);
-            red_shared_u64(smem_u32(&S.blk_hi[bi]), (acc.lo >> 48) | (acc.hi << 16));
-            red_shared_u32(smem_u32(&S.blk_nz[bi]), cnz);
+            red_shared_u64(smem_u32(&S.blk_lo[bi]), lo);
+            red_shared_u64(smem_u32(&S.blk_hi[bi]), hi);
+            red_shared_u32(smem_u32(&S.blk_nz[bi]), z);
           }
           acc.lo = acc.hi = 0ull;
           cnz = 0;
         };
 #pragma unroll 1
-        for (int chunk = 0; chunk < kTileN / 8; ++chunk) {
-          uint32_t v[8];
-          const uint32_t taddr = trow + (uint32_t)(chunk * 8);
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                "=r"(v[6]), "=r"(v[7])
-              : "r"(taddr));
-          tmem_wait_ld8(v);
-          unsigned cnt[8];
-          double dv[8];
+        for (int chunk = col0 / kEpiW; chunk < (col0 + kEpiCols) / kEpiW; ++chunk) {
+          uint32_t v[kEpiW];
+          tmem_ld_w(trow + (uint32_t)(chunk * kEpiW), v);
+          tmem_wait_ld_w(v);
+          // exact integer counts from the FP32 accumulator; c ln c from the
+          // shared 128-bit table, larger counts from the global table
+          unsigned cnt[kEpiW];
+          U128 cv[kEpiW];
+          bool big = false;
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            // exact integer count from the FP32 accumulator
+          for (int q = 0; q < kEpiW; ++q) {
             cnt[q] = __float_as_uint(__uint_as_float(v[q]) + 8388608.0f) - 0x4B000000u;
-            dv[q] = (cnt[q] < (unsigned)kTabTc) ? S.tab[cnt[q]] : clnc_far(gtab, cnt[q]);
+            big |= cnt[q] >= (unsigned)kTabTc;
+            cv[q] = S.tab[min(cnt[q], (unsigned)kTabTc - 1u)];
           }
+          if (__any_sync(0xffffffffu, big)) {
+            // counts beyond the shared table: all loads first, then convert
+            double far[kEpiW];
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            if (chunk * 8 + q == nextb) {
-              flush();
-              ++cs;
-              nextb += nb;
-            }
-            acc = u128_add(acc, u128_from_double(dv[q]));
-            cnz += (cnt[q] != 0u);
+            for (int q = 0; q < kEpiW; ++q)
+              if (cnt[q] >= (unsigned)kTabTc)
+                far[q] = __ldg(gtab + min(cnt[q], (unsigned)kTabGlobal - 1u));
+#pragma unroll
+            for (int q = 0; q < kEpiW; ++q)
+              if (cnt[q] >= (unsigned)kTabTc)
+                cv[q] = (cnt[q] < (unsigned)kTabGlobal) ? u128_from_double(far[q])
+                                                        : clnc_far(cnt[q]);
           }
+          // at most one column DOF boundary per kEpiW columns (nb >= 16):
+          // cells before it close the current segment, the rest open the next
+          const int qb = nextb - chunk * kEpiW;
+          if (qb >= kEpiW) {
+#pragma unroll
+            for (int q = 0; q < kEpiW; ++q) {
+              acc = u128_add(acc, cv[q]);
+              cnz += (cnt[q] != 0u);
+            }
+            continue;
+          }
+          U128 a1;
+          a1.lo = a1.hi = 0ull;
+          unsigned z1 = 0;
+#pragma unroll
+          for (int q = 0; q < kEpiW; ++q) {
+            if (q < qb) {
+              acc = u128_add(acc, cv[q]);
+              cnz += (cnt[q] != 0u);
+            } else {
+              a1 = u128_add(a1, cv[q]);
+              z1 += (cnt[q] != 0u);
+            }
+          }
+          flush();
+          ++cs;
+          nextb += nb;
+          acc = a1;
+          cnz = z1;
         }
         flush();
         named_bar(2, kEpilogue);
-        for (int i = etid; i < kMaxSlotsA * kMaxSlotsB; i += kEpilogue) {
+        for (int i = eth; i < kMaxSlotsA * kMaxSlotsB; i += kEpilogue) {
           const unsigned z = S.blk_nz[i];
           if (z) {
             const int rdb = m.d0a + i / kMaxSlotsB, cdb = m.d0b + i % kMaxSlotsB;
