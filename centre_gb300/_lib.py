@@ -10,7 +10,9 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libcentre_gpu.so")
+# CENTRE_GPU_LIB names another build of the library (e.g. one compiled with
+# different tuning macros); the default is the in-tree build.
+LIB_PATH = os.environ.get("CENTRE_GPU_LIB") or os.path.join(HERE, "libcentre_gpu.so")
 
 SUMS_COLS = 17
 SUMS_NAMES = ["BOND-S1", "ANGLE-S1", "DIHED-S1", "B/B-S2", "B/B-I2", "A/A-S2", "A/A-I2",

@@ -277,12 +277,16 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
       P.nb = nb;
       P.nsteps = E.nsteps;
       const int form = p->counts_form;
-      // AUTO takes the shared-memory histogram whenever its tiles fit: at
-      // these bin counts it outruns the one-hot tensor-core contraction
-      // (B^2 multiply-adds per frame and pair against one increment); the
-      // tensor-core form covers bin counts whose histograms do not fit.
-      const bool use_tc = all && tc_supported(ctx, nb, E.nframes) &&
-                          (form == CENTRE_COUNTS_TC || (form == CENTRE_COUNTS_AUTO && !atomic_fits(nb)));
+      // AUTO takes the tensor-core contraction at its smallest bin count
+      // (16: measured 158 ms against 176 ms for the histogram on all pairs
+      // of 2994 DOFs x 100,000 frames) and where histograms do not fit
+      // shared memory; otherwise the shared-memory histogram, which
+      // outruns the contraction as B^2 multiply-adds per frame and pair
+      // grow against its one increment (20 bins: 233 ms against 150 ms).
+      const bool use_tc =
+          all && tc_supported(ctx, nb, E.nframes) &&
+          (form == CENTRE_COUNTS_TC ||
+           (form == CENTRE_COUNTS_AUTO && (!atomic_fits(nb) || nb <= kTcAutoMaxBins)));
       if (form == CENTRE_COUNTS_TC && !use_tc)
         return set_error(ctx, CENTRE_E_UNSUPPORTED,
                          "tensor-core counts need the all-pairs form and a supported bin count");

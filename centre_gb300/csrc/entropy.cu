@@ -224,6 +224,15 @@ __device__ __forceinline__ uint64_t tri_index(uint64_t i, uint64_t j, uint64_t n
 }
 
 constexpr int kTabHist = 1024;  // 128-bit c ln c entries kept in shared memory
+constexpr int kRedBatch = 4;    // cells per lane per batch in the moment reduction
+#ifndef CENTRE_HIST_MIN_BLOCKS
+#define CENTRE_HIST_MIN_BLOCKS 2
+#endif
+// Resident CTAs per SM the single-trajectory histogram kernel is compiled
+// for (its batched moment reduction needs up to 64 registers).  The batch
+// kernel keeps the one-cell-at-a-time reduction and fewer registers: its
+// autotuned tiles favour more resident CTAs.
+constexpr int kHistMinBlocks = CENTRE_HIST_MIN_BLOCKS;
 
 __device__ __forceinline__ void red_shared_inc(uint32_t addr) {
   asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr) : "memory");
@@ -279,7 +288,7 @@ __device__ void decode_all_pairs_tile(uint64_t id, uint64_t ntile, uint32_t ndof
 // Count all frames of one tile and emit its moments (or counts) per step.
 // `hist` is zeroed on entry and left zeroed.  Returns non-zero if a bin was
 // out of range.  All threads of the CTA call it.
-template <int R, int C, bool kCounts>
+template <int R, int C, bool kCounts, bool kBatchedRed>
 __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_t *cols_s,
                          const uint64_t *out_s, unsigned *hist, const U128 *tab,
                          const double *__restrict__ gtab) {
@@ -292,48 +301,56 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
   // DOF rows as 32-bit word offsets (row starts are 4-byte aligned when the
   // word path is used; the byte path rebuilds the byte offset)
   const uint32_t *bw = reinterpret_cast<const uint32_t *>(bins);
-  uint32_t rw0[R], cw0[C];
-  uint32_t rconst[R], cconst[C];
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    rw0[r] = (uint32_t)((((uint64_t)rows_s[r] * J.nschemes + J.scheme) * n) >> 2);
-    rconst[r] = hist_s + 4u * (uint32_t)(r * C * nb2);
-  }
-#pragma unroll
-  for (int c = 0; c < C; ++c) {
-    cw0[c] = (uint32_t)((((uint64_t)cols_s[c] * J.nschemes + J.scheme) * n) >> 2);
-    cconst[c] = 4u * (uint32_t)(c * nb2);
-  }
   const uint32_t nb4 = 4u * (uint32_t)nb;
   const uint32_t lim = 0x01010101u * (uint32_t)nb;
   const bool word = (n & 3) == 0;
   int bad = 0;
 
-  auto one_frame = [&](uint64_t f) {
-    uint32_t a[R], b[C];
-    bool ok = true;
+
+
+  // row/column word offsets and histogram addresses; with the batched
+  // reduction they are recomputed every step so that none of them is live
+  // across the reduction, which then has the registers to itself
+  uint32_t rw0[R], cw0[C];
+  uint32_t rconst[R], cconst[C];
+  auto setup = [&]() {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      a[r] = bins[((uint64_t)rows_s[r] * J.nschemes + J.scheme) * n + f];
-      ok &= a[r] < (uint32_t)nb;
+      rw0[r] = (uint32_t)((((uint64_t)rows_s[r] * J.nschemes + J.scheme) * n) >> 2);
+      rconst[r] = hist_s + 4u * (uint32_t)(r * C * nb2);
     }
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-      b[c] = bins[((uint64_t)cols_s[c] * J.nschemes + J.scheme) * n + f];
-      ok &= b[c] < (uint32_t)nb;
+      cw0[c] = (uint32_t)((((uint64_t)cols_s[c] * J.nschemes + J.scheme) * n) >> 2);
+      cconst[c] = 4u * (uint32_t)(c * nb2);
     }
-    if (!ok) {
-      bad = 1;
-      return;
-    }
-#pragma unroll
-    for (int r = 0; r < R; ++r)
-#pragma unroll
-      for (int c = 0; c < C; ++c) red_shared_inc(rconst[r] + a[r] * nb4 + cconst[c] + 4u * b[c]);
   };
-
+  if (!kBatchedRed) setup();
   for (int t = 0; t < J.nsteps; ++t) {
     const uint64_t f0 = (uint64_t)t * J.step_size, f1 = f0 + J.step_size;
+    if (kBatchedRed) setup();
+    auto one_frame = [&](uint64_t f) {
+      uint32_t a[R], b[C];
+      bool ok = true;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        a[r] = bins[((uint64_t)rows_s[r] * J.nschemes + J.scheme) * n + f];
+        ok &= a[r] < (uint32_t)nb;
+      }
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        b[c] = bins[((uint64_t)cols_s[c] * J.nschemes + J.scheme) * n + f];
+        ok &= b[c] < (uint32_t)nb;
+      }
+      if (!ok) {
+        bad = 1;
+        return;
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < C; ++c) red_shared_inc(rconst[r] + a[r] * nb4 + cconst[c] + 4u * b[c]);
+    };
     if (word) {
       const uint64_t g0 = (f0 + 3) >> 2, g1 = f1 >> 2;   // whole 4-frame groups
       for (uint64_t f = f0 + tid; f < min(f1, g0 << 2); f += blockDim.x) one_frame(f);
@@ -389,11 +406,47 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
         acc.lo = acc.hi = 0ull;
         unsigned cz = 0;
         const unsigned *h = hist + q * nb2;
-        for (int i = lane; i < nb2; i += 32) {
-          const unsigned c = h[i];
-          const U128 v = (c < (unsigned)kTabHist) ? tab[c] : clnc_far_u128(gtab, c);
-          acc = u128_add(acc, v);
-          cz += (c != 0);
+        if (kBatchedRed) {
+          for (int i0 = 0; i0 < nb2; i0 += 32 * kRedBatch) {
+            // kRedBatch cells per lane: shared-table values first; counts
+            // beyond the table (common at few bins) load from the global table
+            // together
+            unsigned c[kRedBatch];
+            U128 v[kRedBatch];
+            bool far = false;
+  #pragma unroll
+            for (int u = 0; u < kRedBatch; ++u) {
+              const int i = i0 + 32 * u + lane;
+              c[u] = (i < nb2) ? h[i] : 0u;
+              far |= c[u] >= (unsigned)kTabHist;
+              v[u] = tab[min(c[u], (unsigned)kTabHist - 1u)];
+            }
+            if (__any_sync(0xffffffffu, far)) {
+              double fv[kRedBatch];
+  #pragma unroll
+              for (int u = 0; u < kRedBatch; ++u)
+                if (c[u] >= (unsigned)kTabHist)
+                  fv[u] = __ldg(gtab + min(c[u], (unsigned)kTabGlobal - 1u));
+  #pragma unroll
+              for (int u = 0; u < kRedBatch; ++u)
+                if (c[u] >= (unsigned)kTabHist)
+                  v[u] = (c[u] < (unsigned)kTabGlobal) ? u128_from_double(fv[u])
+                                                       : clnc_far_u128(gtab, c[u]);
+            }
+  #pragma unroll
+            for (int u = 0; u < kRedBatch; ++u) {
+              acc = u128_add(acc, v[u]);
+              cz += (c[u] != 0);
+            }
+          }
+        } else {
+          // one cell at a time (fewer registers: more resident CTAs)
+          for (int i = lane; i < nb2; i += 32) {
+            const unsigned c = h[i];
+            const U128 v = (c < (unsigned)kTabHist) ? tab[c] : clnc_far_u128(gtab, c);
+            acc = u128_add(acc, v);
+            cz += (c != 0);
+          }
         }
         for (int off = 16; off; off >>= 1) {
           acc = u128_add(acc, u128_shfl_xor(acc, off));
@@ -414,7 +467,7 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
 }
 
 template <int R, int C, bool kCounts>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, kHistMinBlocks)
 pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__ tasks,
                   const __grid_constant__ PairParams P, const double *__restrict__ gtab,
                   U128 *__restrict__ sclnc, unsigned *__restrict__ nnz,
@@ -453,7 +506,7 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
   J.sclnc = sclnc;
   J.nnz = nnz;
   J.counts = counts;
-  const int bad = hist_tile<R, C, kCounts>(J, rows_s, cols_s, out_s, hist, tab, gtab);
+  const int bad = hist_tile<R, C, kCounts, true>(J, rows_s, cols_s, out_s, hist, tab, gtab);
   if (bad && tid == 0) atomicOr(flag, kFlagBinRange);
 }
 
@@ -502,7 +555,7 @@ pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nit
     J.sclnc = S.sclnc;
     J.nnz = S.nnz;
     J.counts = nullptr;
-    bad |= hist_tile<R, R, false>(J, rows_s, cols_s, out_s, hist, tab, gtab);
+    bad |= hist_tile<R, R, false, false>(J, rows_s, cols_s, out_s, hist, tab, gtab);
   }
   if (bad) atomicOr(flag, kFlagBinRange);
 }

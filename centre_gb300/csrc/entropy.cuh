@@ -185,6 +185,8 @@ size_t vmkde_work_doubles(uint32_t ndof);
 
 // pairs_tc.cu
 bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes);
+// largest bin count at which AUTO prefers the tensor-core contraction
+constexpr int kTcAutoMaxBins = 16;
 int launch_pairs_tc(centre_ctx *ctx, const PairParams &P, const double *d_tab, U128 *d_sclnc,
                     unsigned *d_nnz);
 
