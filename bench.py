@@ -13,6 +13,12 @@ the MIST spanning tree.  Workload: a 1000-atom chain (999 bonds, 998 angles,
 Multi-GPU (torchrun): every rank runs its own independent trajectory
 (replicas; no collective on the data path); value = all ranks' pairs / the
 slowest rank's time.
+
+Besides the contract keys, the line carries `roofline` (the pair-count
+kernel as one-hot-equivalent FLOP/s against the FP8 tensor-core rate: the
+work the contraction form would do), `smem_roofline` (the histogram form
+against its own bound, the shared-memory data pipe) and
+`discretize_roofline` (HBM GB/s).
 """
 from __future__ import annotations
 
@@ -36,9 +42,14 @@ NSTEPS = 10
 
 
 # DRAM bytes per pair of one all-pairs count launch (100,000 frames, 50 bins,
-# 10 steps), from an ncu capture of 176,121 pairs: 61.6 MB read + 14.3 MB
+# 10 steps), from an ncu capture of 176,121 pairs: 60.8 MB read + 14.2 MB
 # written.
-PAIR_TRAFFIC_PER_PAIR = 76.0e6 / 176121
+PAIR_TRAFFIC_PER_PAIR = 75.0e6 / 176121
+# Shared-memory wavefronts per histogram increment of the same capture
+# (2.977e9 wavefronts for 1.761e10 increments: the atomics plus the per-step
+# moment reductions); the data pipe retires one wavefront per SM cycle.
+HIST_WAVEFRONTS_PER_INCREMENT = 2.977e9 / 1.761e10
+SM_COUNT = 152
 
 
 def slowest_rank(value, dist, device="cpu"):
@@ -298,7 +309,7 @@ def run_ours(args):
                      "traffic": PAIR_TRAFFIC_PER_PAIR * npairs,
                      "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu "
                                      "capture of the same kernel on the 594-DOF chain (100,000 "
-                                     "frames, 50 bins, 10 steps): 76.0 MB for 176,121 pairs, "
+                                     "frames, 50 bins, 10 steps): 75.0 MB for 176,121 pairs, "
                                      "scaled by pairs to this launch",
                      "note": f"2*N*B^2 flops per pair (B={NBINS} real bins); fp8 peak = 2 x "
                              f"{src} bf16 {bf16:.0f} TF/s"},
@@ -321,6 +332,17 @@ def run_ours(args):
     clocks = clk.summary()
     if clocks:
         out["clocks"] = clocks
+    if args.form == "atomic" or (args.form == "auto" and NBINS > 16):
+        # the histogram form's own bound: the shared-memory data pipe
+        mhz = (clocks or {}).get("sm_mhz") or 2070.0
+        incr = float(used) * npairs / (pair_ms / 1e3)
+        pipe = SM_COUNT * mhz * 1e6 / HIST_WAVEFRONTS_PER_INCREMENT
+        out["smem_roofline"] = {
+            "bound": "shared-memory data pipe", "kernel": "pair counts (histogram form)",
+            "achieved": incr, "peak": pipe, "unit": "increments/s", "frac": incr / pipe,
+            "note": f"{SM_COUNT} SMs x {mhz:.0f} MHz x 1 wavefront per cycle / "
+                    f"{HIST_WAVEFRONTS_PER_INCREMENT:.3f} wavefronts per increment (ncu capture "
+                    "of the same kernel on the 594-DOF chain)"}
 
     if not args.no_e2e:
         out["e2e"] = run_e2e(ctx, tr, args, w, world, dist, dev)
