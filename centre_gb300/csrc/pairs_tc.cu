@@ -102,12 +102,11 @@ struct TcParams {
   int nsteps;
 };
 
+// Geometry of one 128 x 256 tile of O^T O.
 struct StageMeta {
   int rb, cb;       // tile rows / columns base
   int d0a, nda;     // first DOF and DOF count of the A tile
   int d0b, ndb;
-  int nvalid;       // frames in this chunk
-  int used;
 };
 
 // A producer warp's DOF slot of the current tile: the DOF's bins row
