@@ -118,6 +118,31 @@ class Context:
                                                       _ptr(bins), _ptr(minima), _ptr(nfound)))
         return bins, minima, nfound
 
+    def discretize_gridkde(self, bat_type, data, ngrid, kappa=50.0):
+        """Grid-KDE conformer bins of one DOF-type block [ndof][nframes]
+        (torsions: von Mises kernel of concentration kappa on ngrid points of
+        the circle; bonds/angles: Gaussian kernel, Silverman bandwidth, on
+        ngrid points over the DOF's range) -> (bins [ndof][1][nframes],
+        minima [ndof][ngrid] (first nmin used), nmin [ndof], nbins [ndof])."""
+        data = _c(data, np.float32)
+        ndof, n = data.shape
+        bins = np.empty((ndof, 1, n), np.uint8)
+        minima = np.zeros((ndof, ngrid), np.float64)
+        nmin = np.zeros(ndof, np.uint8)
+        nbins = np.zeros(ndof, np.uint8)
+        self.check(self.L.centre_gpu_discretize_gridkde(self.h, int(bat_type), _ptr(data), ndof, n,
+                                                        int(ngrid), float(kappa), _ptr(bins),
+                                                        _ptr(minima), _ptr(nmin), _ptr(nbins)))
+        return bins, minima, nmin, nbins
+
+    def discretize_gridkde_dev(self, bat_type, data, ngrid, kappa, bins_out, minima_out,
+                               nmin_out, nbins_out):
+        """Device-pointer form of discretize_gridkde (torch CUDA tensors)."""
+        ndof, n = int(data.shape[0]), int(data.shape[1])
+        self.check(self.L.centre_gpu_discretize_gridkde_dev(
+            self.h, int(bat_type), _ptr(data), ndof, n, int(ngrid), float(kappa), _ptr(bins_out),
+            _ptr(minima_out), _ptr(nmin_out), _ptr(nbins_out)))
+
     def entropy1d(self, params: EntropyParams, types, bins, ext, want_freq=False, out=None):
         bins = _c(bins, np.uint8)
         types = _c(types, np.uint8)

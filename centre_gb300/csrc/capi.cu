@@ -831,4 +831,53 @@ int centre_gpu_discretize_vmkde(centre_ctx *ctx, const float *data, uint32_t ndo
   return CENTRE_OK;
 }
 
+int centre_gpu_discretize_gridkde_dev(centre_ctx *ctx, int bat_type, const float *data,
+                                      uint32_t ndof, uint64_t nframes, uint32_t ngrid,
+                                      double kappa, uint8_t *bins, double *minima,
+                                      uint8_t *nmin, uint8_t *nbins) {
+  if (!ctx || ((!data || !bins || !minima || !nmin || !nbins) && ndof && nframes))
+    return set_error(ctx, CENTRE_E_ARG, "null argument");
+  cudaSetDevice(ctx->device);
+  int st = CENTRE_OK;
+  void *d_work = scratch(ctx, kSlotAux, gridkde_work_bytes(ndof) + 16, &st);
+  if (!d_work) return st;
+  CENTRE_TRY(launch_gridkde(ctx, bat_type, data, ndof, nframes, (int)ngrid, kappa, bins, minima,
+                            nmin, nbins, d_work));
+  return read_flag(ctx);
+}
+
+int centre_gpu_discretize_gridkde(centre_ctx *ctx, int bat_type, const float *data,
+                                  uint32_t ndof, uint64_t nframes, uint32_t ngrid, double kappa,
+                                  uint8_t *bins, double *minima, uint8_t *nmin, uint8_t *nbins) {
+  if (!ctx || !data || !bins || !minima || !nmin || !nbins)
+    return set_error(ctx, CENTRE_E_ARG, "null argument");
+  if (ndof == 0 || nframes == 0) return CENTRE_OK;
+  cudaSetDevice(ctx->device);
+  int st = CENTRE_OK;
+  const size_t nin = (size_t)ndof * nframes * 4;
+  unsigned char *d_in = (unsigned char *)scratch(ctx, kSlotIn, nin, &st);
+  if (!d_in) return st;
+  uint8_t *d_bins = (uint8_t *)scratch(ctx, kSlotBins, (size_t)ndof * nframes, &st);
+  if (!d_bins) return st;
+  const size_t nmn = sizeof(double) * (size_t)ndof * ngrid;
+  unsigned char *d_out = (unsigned char *)scratch(ctx, kSlotOut, nmn + 2 * (size_t)ndof + 16, &st);
+  if (!d_out) return st;
+  double *d_min = reinterpret_cast<double *>(d_out);
+  uint8_t *d_nmin = d_out + nmn;
+  uint8_t *d_nb = d_nmin + ndof;
+  void *d_work = scratch(ctx, kSlotAux, gridkde_work_bytes(ndof) + 16, &st);
+  if (!d_work) return st;
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(d_in, data, nin, cudaMemcpyHostToDevice, ctx->stream));
+  CENTRE_TRY(launch_gridkde(ctx, bat_type, (const float *)d_in, ndof, nframes, (int)ngrid, kappa,
+                            d_bins, d_min, d_nmin, d_nb, d_work));
+  CENTRE_TRY(read_flag(ctx));
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(bins, d_bins, (size_t)ndof * nframes, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(minima, d_min, nmn, cudaMemcpyDeviceToHost, ctx->stream));
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(nmin, d_nmin, ndof, cudaMemcpyDeviceToHost, ctx->stream));
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(nbins, d_nb, ndof, cudaMemcpyDeviceToHost, ctx->stream));
+  CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return CENTRE_OK;
+}
+
 }  // extern "C"

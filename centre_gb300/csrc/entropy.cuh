@@ -183,6 +183,12 @@ int launch_vmkde(centre_ctx *ctx, const float *d_data, uint32_t ndof, uint64_t n
                  double *d_work);
 size_t vmkde_work_doubles(uint32_t ndof);
 
+// gridkde.cu
+int launch_gridkde(centre_ctx *ctx, int bat_type, const float *d_data, uint32_t ndof,
+                   uint64_t nframes, int ngrid, double kappa, uint8_t *d_bins, double *d_minima,
+                   uint8_t *d_nmin, uint8_t *d_nbins, void *d_work);
+size_t gridkde_work_bytes(uint32_t ndof);
+
 // pairs_tc.cu
 bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes);
 // largest bin count at which AUTO prefers the tensor-core contraction

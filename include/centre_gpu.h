@@ -133,6 +133,28 @@ int centre_gpu_discretize_vmkde(centre_ctx *ctx, const float *data,
                                 uint32_t sdo_niter, uint8_t *bins,
                                 double *minima, uint8_t *nfound);
 
+/* Grid-KDE conformer binning of one DOF-type block (bat_type 1 bonds, 2
+ * angles, 3 torsions), a KDE variant with no reference counterpart beside
+ * centre_gpu_discretize_vmkde (which follows Real2Int::getMinimaPositions,
+ * src/Real2Int.cpp:481, for torsions only).  Torsions: von Mises kernel
+ * exp(kappa (cos(g - a) - 1)) on ngrid points g_j = 2 pi j / ngrid.  Bonds and
+ * angles: Gaussian kernel with h = 1.06 sigma N^(-1/5) on ngrid points
+ * lo + (j + 1/2)(hi - lo)/ngrid (kappa unused).  Grid minima
+ * (d_j < d_{j-1}, d_j <= d_{j+1}, cyclic for torsions) bound the conformer
+ * intervals; bins [ndof][nframes] = interval index (linear: #minima <= x;
+ * torsions: (#{minima <= a} + M - 1) mod M).  minima [ndof][ngrid] (first
+ * nmin[d] used), nbins [ndof] = bins used by the DOF.  ngrid 3..128.  Grid
+ * sums are FP64; non-finite inputs give CENTRE_E_ARG.  Entropies of these
+ * bins take the KDE form (bin width 1), as for the reference's KDE. */
+int centre_gpu_discretize_gridkde(centre_ctx *ctx, int bat_type, const float *data,
+                                  uint32_t ndof, uint64_t nframes, uint32_t ngrid,
+                                  double kappa, uint8_t *bins, double *minima,
+                                  uint8_t *nmin, uint8_t *nbins);
+int centre_gpu_discretize_gridkde_dev(centre_ctx *ctx, int bat_type, const float *data,
+                                      uint32_t ndof, uint64_t nframes, uint32_t ngrid,
+                                      double kappa, uint8_t *bins, double *minima,
+                                      uint8_t *nmin, uint8_t *nbins);
+
 /* ------------------------------------------------------------ entropy ---- */
 /* 1-D counts and entropies: binData1D (src/Estimators.cpp:56) + entropy1D
  * (:217) for every DOF, as EntropyCalculator::run1d (EntropyCalculator.cpp:
