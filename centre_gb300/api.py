@@ -186,7 +186,7 @@ class Context:
 
     def pair_moments(self, params: EntropyParams, bins, scheme=0):
         """Integer moments of every pair i<j: (clnc [npairs][nsteps][2] uint64
-        as (low, high) words of sum c ln c * 2^60, nnz [npairs][nsteps])."""
+        as (low, high) words of sum c ln c * 2^52, nnz [npairs][nsteps])."""
         bins = _c(bins, np.uint8)
         ndof = bins.shape[0]
         npairs = ndof * (ndof - 1) // 2

@@ -18,7 +18,7 @@ constexpr int kMaxSchemes = 16;
 constexpr int kMaxSteps = 255;
 
 // Largest frame count: counts stay below 2^27, so a per-pair sum of up to
-// 65025 cells of c ln c * 2^60 fits in 128 bits.
+// 65025 cells of c ln c * 2^52 fits in 128 bits.
 constexpr uint64_t kMaxFrames = 1ull << 27;
 
 // Grow-only device scratch owned by a context.

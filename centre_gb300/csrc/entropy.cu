@@ -224,6 +224,7 @@ __device__ __forceinline__ uint64_t tri_index(uint64_t i, uint64_t j, uint64_t n
 }
 
 constexpr int kTabHist = 1024;  // 128-bit c ln c entries kept in shared memory
+constexpr int kTab64 = 512;     // c ln c * 2^52 < 2^64 for these counts: 64-bit entries
 constexpr int kRedBatch = 4;    // cells per lane per batch in the moment reduction
 #ifndef CENTRE_HIST_MIN_BLOCKS
 #define CENTRE_HIST_MIN_BLOCKS 2
@@ -291,7 +292,7 @@ __device__ void decode_all_pairs_tile(uint64_t id, uint64_t ntile, uint32_t ndof
 template <int R, int C, bool kCounts, bool kBatchedRed>
 __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_t *cols_s,
                          const uint64_t *out_s, unsigned *hist, const U128 *tab,
-                         const double *__restrict__ gtab) {
+                         const unsigned long long *tab64, const double *__restrict__ gtab) {
   constexpr int NP = R * C;
   const int tid = threadIdx.x;
   const int nb = J.nb, nb2 = nb * nb;
@@ -408,32 +409,35 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
         const unsigned *h = hist + q * nb2;
         if (kBatchedRed) {
           for (int i0 = 0; i0 < nb2; i0 += 32 * kRedBatch) {
-            // kRedBatch cells per lane: shared-table values first; counts
-            // beyond the table (common at few bins) load from the global table
-            // together
+            // kRedBatch cells per lane: counts below kTab64 from the 64-bit
+            // shared table (half the bytes of the 128-bit one: the data pipe
+            // bounds this kernel), the rest from the 128-bit table or, beyond
+            // it (common at few bins), from the global table, loaded together
             unsigned c[kRedBatch];
             U128 v[kRedBatch];
-            bool far = false;
-  #pragma unroll
+            bool big = false;
+#pragma unroll
             for (int u = 0; u < kRedBatch; ++u) {
               const int i = i0 + 32 * u + lane;
               c[u] = (i < nb2) ? h[i] : 0u;
-              far |= c[u] >= (unsigned)kTabHist;
-              v[u] = tab[min(c[u], (unsigned)kTabHist - 1u)];
+              big |= c[u] >= (unsigned)kTab64;
+              v[u].lo = tab64[min(c[u], (unsigned)kTab64 - 1u)];
+              v[u].hi = 0ull;
             }
-            if (__any_sync(0xffffffffu, far)) {
+            if (__any_sync(0xffffffffu, big)) {
               double fv[kRedBatch];
-  #pragma unroll
+#pragma unroll
               for (int u = 0; u < kRedBatch; ++u)
                 if (c[u] >= (unsigned)kTabHist)
                   fv[u] = __ldg(gtab + min(c[u], (unsigned)kTabGlobal - 1u));
-  #pragma unroll
+#pragma unroll
               for (int u = 0; u < kRedBatch; ++u)
-                if (c[u] >= (unsigned)kTabHist)
-                  v[u] = (c[u] < (unsigned)kTabGlobal) ? u128_from_double(fv[u])
-                                                       : clnc_far_u128(gtab, c[u]);
+                if (c[u] >= (unsigned)kTab64)
+                  v[u] = (c[u] < (unsigned)kTabHist)    ? tab[c[u]]
+                         : (c[u] < (unsigned)kTabGlobal) ? u128_from_double(fv[u])
+                                                          : clnc_far_u128(gtab, c[u]);
             }
-  #pragma unroll
+#pragma unroll
             for (int u = 0; u < kRedBatch; ++u) {
               acc = u128_add(acc, v[u]);
               cz += (c[u] != 0);
@@ -477,6 +481,7 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
   const int nb2 = P.nb * P.nb;
   unsigned *hist = reinterpret_cast<unsigned *>(dyn);
   U128 *tab = reinterpret_cast<U128 *>(dyn + (((size_t)NP * nb2 * 4 + 15) & ~size_t(15)));
+  unsigned long long *tab64 = reinterpret_cast<unsigned long long *>(tab + kTabHist);
   __shared__ uint32_t rows_s[R], cols_s[C];
   __shared__ uint64_t out_s[NP];
   const int tid = threadIdx.x;
@@ -493,6 +498,7 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
     }
   }
   for (int i = tid; i < kTabHist; i += blockDim.x) tab[i] = u128_from_double(__ldg(gtab + i));
+  for (int i = tid; i < kTab64; i += blockDim.x) tab64[i] = u128_from_double(__ldg(gtab + i)).lo;
   for (int i = tid; i < NP * nb2; i += blockDim.x) hist[i] = 0;
   __syncthreads();
   HistJob J;
@@ -506,7 +512,8 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
   J.sclnc = sclnc;
   J.nnz = nnz;
   J.counts = counts;
-  const int bad = hist_tile<R, C, kCounts, true>(J, rows_s, cols_s, out_s, hist, tab, gtab);
+  const int bad =
+      hist_tile<R, C, kCounts, true>(J, rows_s, cols_s, out_s, hist, tab, tab64, gtab);
   if (bad && tid == 0) atomicOr(flag, kFlagBinRange);
 }
 
@@ -555,7 +562,7 @@ pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nit
     J.sclnc = S.sclnc;
     J.nnz = S.nnz;
     J.counts = nullptr;
-    bad |= hist_tile<R, R, false, false>(J, rows_s, cols_s, out_s, hist, tab, gtab);
+    bad |= hist_tile<R, R, false, false>(J, rows_s, cols_s, out_s, hist, tab, nullptr, gtab);
   }
   if (bad) atomicOr(flag, kFlagBinRange);
 }
@@ -855,7 +862,8 @@ template <int R, int C>
 static int launch_hist(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
                        uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
                        unsigned *d_counts) {
-  const size_t smem = (((size_t)R * C * P.nb * P.nb * 4 + 15) & ~size_t(15)) + 16 * kTabHist;
+  const size_t smem =
+      (((size_t)R * C * P.nb * P.nb * 4 + 15) & ~size_t(15)) + 16 * kTabHist + 8 * kTab64;
   if (d_counts) {
     CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, true>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -96,11 +96,13 @@ __device__ __forceinline__ double clnc_value(unsigned c) {
 }
 
 // A non-negative double v (0 or >= 1) represented exactly as an integer
-// multiple of 2^-60: its 53-bit significand shifted by its exponent (v >= 1
-// gives a shift >= 60 - 52 = 8, so it is a left shift and nothing is
-// rounded).  Integer sums of these are the exact sums of the per-cell
-// doubles, so the cell sum is independent of how cells are spread over
-// threads, tiles or count kernels.
+// multiple of 2^-52: its 53-bit significand shifted by its exponent (a double
+// >= 1 is a multiple of its ulp >= 2^-52, so the shift is a left shift and
+// nothing is rounded).  Integer sums of these are the exact sums of the
+// per-cell doubles, so the cell sum is independent of how cells are spread
+// over threads, tiles or count kernels.  c ln c < 2^12 (counts below 630)
+// fits in the low word alone.
+constexpr int kFixShift = 52;   // fixed point: value * 2^52
 __device__ __forceinline__ U128 u128_from_double(double v) {
   U128 r;
   r.lo = 0ull;
@@ -108,13 +110,14 @@ __device__ __forceinline__ U128 u128_from_double(double v) {
   // integer test for +-0 (no FP64 instruction: FP64 issue is scarce on this part)
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
   if ((bits << 1) == 0ull) return r;
-  const int s = (int)((bits >> 52) & 0x7ff) - 1023 + 8;  // value = m * 2^(e - 52 + 60)
+  // value * 2^52 = m * 2^(e - 1023), e the biased exponent
+  const int s = (int)((bits >> 52) & 0x7ff) - 1023 + (kFixShift - 52);
   const unsigned long long m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
   if (s >= 64) {
     r.hi = m << (s - 64);
   } else {
     r.lo = m << s;
-    r.hi = m >> (64 - s);
+    r.hi = s ? (m >> (64 - s)) : 0ull;
   }
   return r;
 }
@@ -138,7 +141,7 @@ __device__ __forceinline__ void tri_pair(uint64_t p, uint64_t n, uint32_t &i, ui
 }
 
 __host__ __device__ __forceinline__ double u128_value(U128 x) {
-  return (double)x.hi * 16.0 + (double)x.lo * 0x1p-60;
+  return (double)x.hi * 0x1p12 + (double)x.lo * 0x1p-52;
 }
 
 int init_clnc_table(centre_ctx *ctx, double *tab);

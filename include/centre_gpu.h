@@ -217,7 +217,7 @@ int centre_gpu_counts2d(centre_ctx *ctx, const centre_entropy_params *p,
  * as both count forms produce them (no reference counterpart: the
  * reference keeps the counts themselves, src/Estimators.cpp:130-205, and sums
  * p log p in entropy2D, :586-631).  Per pair and step: sum over cells of
- * c*ln(c) as an unsigned 128-bit integer in units of 2^-60 (clnc[2*k] low,
+ * c*ln(c) as an unsigned 128-bit integer in units of 2^-52 (clnc[2*k] low,
  * clnc[2*k+1] high word) and the number of non-empty cells.  Used to check
  * that the tensor-core and atomic forms count identically.
  *   clnc [npairs][nsteps][2] uint64, nnz [npairs][nsteps] uint32. */

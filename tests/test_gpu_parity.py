@@ -371,7 +371,7 @@ def test_tc_counts_identical_to_atomic(gpu, orc, natoms, nframes, nsteps, nb):
     ct, zt = gpu.pair_moments(pt, bins)
     xo, zo = oracle_moments(orc, bins[:, 0], nsteps, nb)
     assert np.array_equal(zt, zo)
-    xt = ct[..., 1].astype(np.float64) * 16.0 + ct[..., 0].astype(np.float64) * 2.0 ** -60
+    xt = ct[..., 1].astype(np.float64) * 2.0 ** 12 + ct[..., 0].astype(np.float64) * 2.0 ** -52
     np.testing.assert_allclose(xt, xo, rtol=1e-12)
     if nb * nb * 4 <= 200 * 1024:
         assert np.array_equal(ct, ca) and np.array_equal(zt, za)
