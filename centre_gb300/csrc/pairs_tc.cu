@@ -31,15 +31,16 @@
 // adding them into the pair's moments with integer atomics (tiles split pair
 // blocks; integer addition keeps the result independent of the split).
 //
-// Warp roles (544 threads): warp 0 allocates TMEM and one lane issues the
+// Warp roles (672 threads): warp 0 allocates TMEM and one lane issues the
 // MMAs; warps 1-12 produce operand stages, three per stage (warp 1+p+4h marks
-// the DOF slots h, h+3, ... of stage p), so the four stages are built
-// concurrently without cross-warp barriers, each warp prefetching the bins of
-// its next chunk into registers while it marks the current one (the marking
-// is bound by instruction issue and latency; more warps hide it); warps 13-16
-// run the epilogue (TMEM lane group = warp % 4).  Every mbarrier wait is
-// bounded: on expiry the kernel sets an error flag, lets the MMAs it issued
-// drain (again bounded), frees its TMEM and returns.
+// the DOF slots h, h+3, ... of stage p, from a per-tile slot table in shared
+// memory), so the four stages are built concurrently without cross-warp
+// barriers, each warp prefetching the bins of its next chunk into registers
+// while it marks the current one (the marking is bound by instruction issue
+// and latency; more warps hide it); warps 13-20 run the epilogue as two
+// quartets over the two column halves (TMEM lane group = warp % 4).  Every
+// mbarrier wait is bounded: on expiry the kernel sets an error flag, lets the
+// MMAs it issued drain (again bounded), frees its TMEM and returns.
 #include <algorithm>
 #include <vector>
 
