@@ -355,6 +355,19 @@ bool Inputs::derive(std::string *err) {
         {kAD2D, "entcontri_ad-2d.nc"}};
     for (const auto &f : files)
       if (ws & f.first) unwanted_files.push_back(join(control.outfilepath, f.second));
+    // histogram dumps (Inputs.cpp:826-872: the bond-bond file is listed by
+    // the write set alone)
+    if (hist.writefreq) {
+      const uint32_t hs = hist.writeset;
+      const std::pair<uint32_t, const char *> hfiles[] = {
+          {hs & ws & kB1D, "hist_bnd-1d.nc"}, {hs & ws & kA1D, "hist_ang-1d.nc"},
+          {hs & ws & kD1D, "hist_tor-1d.nc"}, {hs & kBB2D, "hist_bnd-2d.nc"},
+          {hs & ws & kAA2D, "hist_ang-2d.nc"}, {hs & ws & kDD2D, "hist_tor-2d.nc"},
+          {hs & ws & kBA2D, "hist_ba-2d.nc"}, {hs & ws & kBD2D, "hist_bd-2d.nc"},
+          {hs & ws & kAD2D, "hist_ad-2d.nc"}};
+      for (const auto &f : hfiles)
+        if (f.first) unwanted_files.push_back(join(control.outfilepath, f.second));
+    }
   }
   return true;
 }

@@ -111,6 +111,81 @@ bool write_entcontri(const std::string &path, const std::string &content, int or
   return nc_write(path, o, err);
 }
 
+// hist_*.nc: the counts behind the entropies, written when [histogram]
+// writefreq is on (Netcdf_HistUtil, src/Netcdf_HistUtils.cpp:217-270 for the
+// sizes and :804-1029 for the header; records as EntropyCalculator::run1d /
+// run2d_xx / run2d_xy fill them, src/EntropyCalculator.cpp:176-186,
+// :575-586).  As in the reference, the ubyte diagonal flag is written under
+// the attribute name "title" (over the text title) and the application
+// attribute is spelled "appication".  Records: id [ndims], extrema
+// [ndims][4], bin mids [ndims * sum nb], cumulative counts of the written
+// steps [nsteps_eff][sum nb^ndims].
+struct HistSteps {
+  int first, stride, neff;
+};
+
+HistSteps hist_steps(const Inputs &in, int nsteps) {
+  // Netcdf_HistUtil's clamping (src/Netcdf_HistUtils.cpp:227-232)
+  HistSteps h;
+  const int ns = nsteps < 1 ? 1 : nsteps;
+  const int first = in.hist.writestepstart;
+  h.first = (first < 0 || first >= ns) ? ns - 1 : first;
+  const int st = in.hist.writestepstride;
+  h.stride = st < 1 ? 1 : (st > ns ? ns : st);
+  h.neff = (ns - h.first + h.stride - 1) / h.stride;
+  return h;
+}
+
+// bin mids of one DOF for every scheme: binData1D's running offset
+// (src/Estimators.cpp:67-77)
+void append_mids(double mn, double mx, const std::vector<uint8_t> &schemes,
+                 std::vector<double> &out) {
+  for (uint8_t nb : schemes) {
+    const double w = (mx - mn) / nb, half = w / 2.0;
+    double off = mn;
+    for (int i = 0; i < nb; ++i) {
+      out.push_back(off + half);
+      off += w;
+    }
+  }
+}
+
+bool write_hist(const std::string &path, const std::string &content, int ndims,
+                const HistSteps &hs, int nsteps, const std::vector<uint64_t> &dim_lens,
+                uint8_t storage, const std::vector<uint8_t> &schemes,
+                const std::vector<uint32_t> &ids, const std::vector<double> &extrema,
+                const std::vector<double> &mids, const std::vector<uint64_t> &freq,
+                std::string *err) {
+  uint64_t sum = 0, pow_sum = 0;
+  for (uint8_t nb : schemes) {
+    sum += nb;
+    pow_sum += ndims == 1 ? nb : (uint64_t)nb * nb;
+  }
+  NcOut o;
+  o.version = 5;
+  o.dims = {{"records", 0}, {"dimsXbin_sum", sum * ndims}, {"bin_pow_dims_sum", pow_sum},
+            {"nsteps_eff", (uint64_t)hs.neff}, {"ids", (uint64_t)ndims}, {"extremes", 4}};
+  o.atts = {NcAtt::values<uint8_t>("title", kNcUByte, {(uint8_t)(storage != 0 ? 1 : 0)}),
+            NcAtt::text("appication", "CENTRE"), NcAtt::text("program", "Real2Int"),
+            NcAtt::text("programVersion", "1.0.0"), NcAtt::text("convention", "CENTRE_HIST"),
+            NcAtt::text("conventionVersion", "1.0"), NcAtt::text("content", content),
+            NcAtt::values<uint8_t>("order", kNcUByte, {(uint8_t)ndims}),
+            NcAtt::values<uint8_t>("firstStep", kNcUByte, {(uint8_t)hs.first}),
+            NcAtt::values<uint8_t>("nsteps", kNcUByte, {(uint8_t)(nsteps < 1 ? 1 : nsteps)}),
+            NcAtt::values<uint8_t>("stepStride", kNcUByte, {(uint8_t)hs.stride}),
+            NcAtt::values<uint8_t>("storagetype", kNcUByte, {storage}),
+            NcAtt::values<uint8_t>("ndims", kNcUByte, {(uint8_t)ndims}),
+            NcAtt::values<uint64_t>("dimLengths", kNcUInt64, dim_lens),
+            NcAtt::values<uint8_t>("nbinSchemes", kNcUByte, {(uint8_t)schemes.size()}),
+            NcAtt::values<uint8_t>("binSchemes", kNcUByte, schemes)};
+  o.vars = {{"id", {0, 4}, {}, kNcUInt, ids.data()},
+            {"extrema", {0, 4, 5}, {}, kNcDouble, extrema.data()},
+            {"mid", {0, 1}, {}, kNcDouble, mids.data()},
+            {"freq", {0, 3, 2}, {}, kNcUInt64, freq.data()}};
+  o.numrecs = ids.size() / (size_t)ndims;
+  return nc_write(path, o, err);
+}
+
 struct EntFile {
   std::vector<uint32_t> ids;       // [rec][order]
   std::vector<double> contri;      // [rec][G]
@@ -364,18 +439,30 @@ bool EntropyCalculator::run(std::string *err) {
   centre_entropy_params p = make_params(in_);
   const uint64_t G = (uint64_t)p.nestimators * p.nschemes * p.nsteps;
   std::vector<double> s1((size_t)ndof * G);
+  const bool dump = in_.hist.writefreq;
+  const uint32_t dumpset = in_.hist.writeset;
+  const HistSteps hs = hist_steps(in_, p.nsteps);
+  uint64_t nbsum = 0, nb2sum = 0;
+  for (uint8_t nb : in_.hist.bin_schemes) {
+    nbsum += nb;
+    nb2sum += (uint64_t)nb * nb;
+  }
+  std::vector<uint64_t> freq1;
+  if (dump) freq1.resize((size_t)ndof * p.nsteps * nbsum);
   int rc = centre_gpu_entropy1d(gpu_.ctx(), &p, ndof, types.data(), bins.data(), ext.data(),
-                                s1.data(), nullptr);
+                                s1.data(), dump ? freq1.data() : nullptr);
   if (rc != CENTRE_OK) return fail(err, gpu_.error(rc, "1-D entropies"));
   // 1-D files: records in subset order (EntropyCalculator::run1d)
   struct OneD {
     uint32_t set;
     int t;
     const std::vector<uint32_t> *ids;
-    const char *file, *content;
-  } oned[3] = {{kB1D | kBB2D, 0, &ss.bonds, "entcontri_bnd-1d.nc", "B"},
-               {kA1D | kAA2D, 1, &ss.angles, "entcontri_ang-1d.nc", "A"},
-               {kD1D | kDD2D, 2, &ss.torsions, "entcontri_tor-1d.nc", "D"}};
+    const char *file, *content, *hfile;
+    uint32_t hset;
+  } oned[3] = {{kB1D | kBB2D, 0, &ss.bonds, "entcontri_bnd-1d.nc", "B", "hist_bnd-1d.nc", kB1D},
+               {kA1D | kAA2D, 1, &ss.angles, "entcontri_ang-1d.nc", "A", "hist_ang-1d.nc", kA1D},
+               {kD1D | kDD2D, 2, &ss.torsions, "entcontri_tor-1d.nc", "D", "hist_tor-1d.nc",
+                kD1D}};
   for (const OneD &o : oned) {
     if (!(ws & o.set)) continue;
     std::vector<uint32_t> ids = *o.ids;
@@ -388,19 +475,37 @@ bool EntropyCalculator::run(std::string *err) {
     if (!write_entcontri(out_path(in_, o.file), o.content, 1, {(uint64_t)ids.size()},
                          p.nsteps, in_.hist.bin_schemes, p.nestimators, ids, contri, err))
       return false;
+    if (dump && (dumpset & ws & o.hset)) {
+      std::vector<double> extrema, mids;
+      std::vector<uint64_t> freq;
+      for (uint32_t id : ids) {
+        const uint32_t i = index_of[o.t][id];
+        extrema.insert(extrema.end(), &ext[(size_t)i * 4], &ext[(size_t)i * 4] + 4);
+        append_mids(ext[(size_t)i * 4], ext[(size_t)i * 4 + 1], in_.hist.bin_schemes, mids);
+        for (int k = 0; k < hs.neff; ++k) {
+          const uint64_t *row =
+              &freq1[((size_t)i * p.nsteps + hs.first + (size_t)k * hs.stride) * nbsum];
+          freq.insert(freq.end(), row, row + nbsum);
+        }
+      }
+      if (!write_hist(out_path(in_, o.hfile), o.content, 1, hs, p.nsteps,
+                      {(uint64_t)ids.size()}, 0, in_.hist.bin_schemes, ids, extrema, mids, freq,
+                      err))
+        return false;
+    }
   }
   // 2-D: every pair list, one GPU call
   struct TwoD {
     uint32_t set;
     int tx, ty;
     const std::map<uint32_t, std::vector<uint32_t>> *m;
-    const char *file, *content;
-  } twod[6] = {{kBB2D, 0, 0, &nb.bb, "entcontri_bnd-2d.nc", "B/B"},
-               {kAA2D, 1, 1, &nb.aa, "entcontri_ang-2d.nc", "A/A"},
-               {kDD2D, 2, 2, &nb.dd, "entcontri_tor-2d.nc", "D/D"},
-               {kBA2D, 0, 1, &nb.ba, "entcontri_ba-2d.nc", "B/A"},
-               {kBD2D, 0, 2, &nb.bd, "entcontri_bd-2d.nc", "B/D"},
-               {kAD2D, 1, 2, &nb.ad, "entcontri_ad-2d.nc", "A/D"}};
+    const char *file, *content, *hfile;
+  } twod[6] = {{kBB2D, 0, 0, &nb.bb, "entcontri_bnd-2d.nc", "B/B", "hist_bnd-2d.nc"},
+               {kAA2D, 1, 1, &nb.aa, "entcontri_ang-2d.nc", "A/A", "hist_ang-2d.nc"},
+               {kDD2D, 2, 2, &nb.dd, "entcontri_tor-2d.nc", "D/D", "hist_tor-2d.nc"},
+               {kBA2D, 0, 1, &nb.ba, "entcontri_ba-2d.nc", "B/A", "hist_ba-2d.nc"},
+               {kBD2D, 0, 2, &nb.bd, "entcontri_bd-2d.nc", "B/D", "hist_bd-2d.nc"},
+               {kAD2D, 1, 2, &nb.ad, "entcontri_ad-2d.nc", "A/D", "hist_ad-2d.nc"}};
   std::vector<uint32_t> pairs;                 // [npairs][2] array indices
   std::vector<size_t> block_start(7, 0);
   bool ordered = true;
@@ -453,6 +558,42 @@ bool EntropyCalculator::run(std::string *err) {
     if (!write_entcontri(out_path(in_, twod[b].file), twod[b].content, 2, {nx, ny}, p.nsteps,
                          in_.hist.bin_schemes, p.nestimators, ids, contri, err))
       return false;
+    if (dump && (dumpset & ws & twod[b].set) && q1 > q0) {
+      // joint counts of the block's pairs, a bounded number of pairs per call
+      const uint64_t per_pair = (uint64_t)p.nsteps * nb2sum;
+      const uint64_t chunk = std::max<uint64_t>(1, (uint64_t(1) << 27) / per_pair);
+      std::vector<uint64_t> cnt, freq;
+      std::vector<double> extrema, mids;
+      freq.reserve((q1 - q0) * (size_t)hs.neff * nb2sum);
+      for (uint64_t c0 = q0; c0 < q1; c0 += chunk) {
+        const uint64_t nc = std::min<uint64_t>(chunk, q1 - c0);
+        cnt.resize(nc * per_pair);
+        rc = centre_gpu_counts2d(gpu_.ctx(), &p, ndof, bins.data(), nc, &pairs[2 * c0],
+                                 cnt.data());
+        if (rc != CENTRE_OK) return fail(err, gpu_.error(rc, "2-D histograms"));
+        for (uint64_t q = 0; q < nc; ++q)
+          for (int k = 0; k < hs.neff; ++k) {
+            const uint64_t *row =
+                &cnt[(q * p.nsteps + hs.first + (size_t)k * hs.stride) * nb2sum];
+            freq.insert(freq.end(), row, row + nb2sum);
+          }
+      }
+      for (uint64_t q = q0; q < q1; ++q) {
+        const uint32_t i = pairs[2 * q], j = pairs[2 * q + 1];
+        extrema.insert(extrema.end(), &ext[(size_t)i * 4], &ext[(size_t)i * 4] + 4);
+        extrema.insert(extrema.end(), &ext[(size_t)j * 4], &ext[(size_t)j * 4] + 4);
+        // per scheme: the first DOF's mids, then the second's (binData2D)
+        for (uint8_t nbk : in_.hist.bin_schemes) {
+          const std::vector<uint8_t> one(1, nbk);
+          append_mids(ext[(size_t)i * 4], ext[(size_t)i * 4 + 1], one, mids);
+          append_mids(ext[(size_t)j * 4], ext[(size_t)j * 4 + 1], one, mids);
+        }
+      }
+      const uint8_t storage = twod[b].tx == twod[b].ty ? 0 : 3;   // FULL / UPPER
+      if (!write_hist(out_path(in_, twod[b].hfile), twod[b].content, 2, hs, p.nsteps, {nx, ny},
+                      storage, in_.hist.bin_schemes, ids, extrema, mids, freq, err))
+        return false;
+    }
   }
   (void)S;
   (void)nfr;

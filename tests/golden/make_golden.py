@@ -22,7 +22,12 @@ stores inputs and outputs:
                       hdf5_min.py): the reference's own 1-D and 2-D entropies
                       of the subset DOFs and neighbour pairs
 
+  hist_tor1d_ref.json/.npz  header and first records of the reference's
+                      histogram dump test_examples/example-2/outfiles-h-ref/
+                      hist_tor-1d.nc
+
     python tests/golden/make_golden.py example1     # only the example-1 fixtures
+    python tests/golden/make_golden.py hist         # only the histogram-dump fixture
 """
 from __future__ import annotations
 
@@ -186,9 +191,37 @@ def make_example1():
     np.savez_compressed(os.path.join(HERE, "example1_entcontri.npz"), **ent)
 
 
+def make_hist():
+    """Header and first records of the reference's histogram dump
+    test_examples/example-2/outfiles-h-ref/hist_tor-1d.nc (CDF-5, written by
+    Netcdf_HistUtil, src/Netcdf_HistUtils.cpp:804-1029): attribute names,
+    types and values in file order, dimensions, variables, and the id,
+    extrema, mid and freq of the first 16 records."""
+    from centre_gb300 import cdf5
+    path = os.path.join(REF, "test_examples", "example-2", "outfiles-h-ref", "hist_tor-1d.nc")
+    ds = cdf5.read(path)
+    atts = []
+    for k, v in ds.attrs.items():
+        if isinstance(v, str):
+            atts.append([k, "text", v])
+        else:
+            atts.append([k, str(v.dtype.newbyteorder("=").name), [int(x) for x in v]])
+    out = {"version": int(ds.version), "numrecs": int(ds.numrecs), "atts": atts,
+           "dims": [[k, int(n)] for k, n in ds.dims.items()],
+           "vars": [[v.name, list(v.dims), int(v.nctype)] for v in ds.vars.values()]}
+    with open(os.path.join(HERE, "hist_tor1d_ref.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    np.savez_compressed(os.path.join(HERE, "hist_tor1d_ref.npz"),
+                        id=ds.vars["id"].data[:16], extrema=ds.vars["extrema"].data[:16],
+                        mid=ds.vars["mid"].data[:16], freq=ds.vars["freq"].data[:16])
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["example1"]:
         make_example1()
+        sys.exit(0)
+    if sys.argv[1:] == ["hist"]:
+        make_hist()
         sys.exit(0)
     oracle.build(with_ref=True)
     R = oracle.Reference()
@@ -197,4 +230,5 @@ if __name__ == "__main__":
     make_mst(R)
     make_vmkde(R)
     make_example1()
+    make_hist()
     print("fixtures written to", HERE)

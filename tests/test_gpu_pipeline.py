@@ -272,3 +272,97 @@ def test_pipeline_learned_neighbours(gpu, tmp_path):
     _, rows_learn = read_csv(out / "MIST-ML_convergence_b-30.csv")
     s_full, s_learn = float(rows_full[-1][-1]), float(rows_learn[-1][-1])
     assert abs(s_learn - s_full) <= 0.01 * abs(s_full)
+
+
+def test_pipeline_histogram_dumps(gpu, tmp_path):
+    """[histogram] writefreq: hist_*.nc with the reference's header layout
+    (pinned by its own example-2 dump) and the counts of the written steps."""
+    import json
+    from conftest import GOLDEN
+    tr = chain_trajectory(8, 4003, seed=31)
+    body = BODY.replace("    nbins = 30, 20\n",
+                        "    nbins = 30, 20\n    writefreq = true\n"
+                        "    writeset = B1D, A1D, D1D, BB2D, AA2D, DD2D, BA2D, BD2D, AD2D\n"
+                        "    writestepstart = 1\n    writestepstride = 2\n")
+    out = case(tmp_path, tr, body)
+    ref = json.load(open(os.path.join(GOLDEN, "hist_tor1d_ref.json")))
+    sch = [30, 20]
+    n = tr.nframes
+    step = n // 4
+    steps = [1, 3]                                   # first 1, stride 2 of 4 steps
+    bins, ext = {}, {}
+    for typ in (1, 2, 3):
+        _, e, c, _ = cdf5.read_bins(str(out / f"bin_{NAMES[typ]}.nc"))
+        bins[typ], ext[typ] = c, e
+
+    def mids1(e, nb):
+        # binData1D's running offset (src/Estimators.cpp:67-77)
+        m = []
+        w = (e[1] - e[0]) / nb
+        half, off = w / 2.0, e[0]
+        for _ in range(nb):
+            m.append(off + half)
+            off += w
+        return m
+
+    def mids(e):
+        return np.array(sum((mids1(e, nb) for nb in sch), []))
+
+    def check_header(ds, content, ndims, storage, dim_lens):
+        # attribute names, order and types as the reference writes them
+        got = [(k, "text" if isinstance(v, str) else v.dtype.newbyteorder("=").name)
+               for k, v in ds.attrs.items()]
+        assert got == [(a[0], a[1]) for a in ref["atts"]]
+        for a in ref["atts"]:
+            if a[0] in ("appication", "program", "programVersion", "convention",
+                        "conventionVersion"):
+                assert ds.attrs[a[0]] == a[2]
+        assert ds.attrs["content"] == content
+        assert ds.attrs["title"].tolist() == [1 if storage else 0]
+        assert ds.attrs["order"].tolist() == [ndims] and ds.attrs["ndims"].tolist() == [ndims]
+        assert ds.attrs["firstStep"].tolist() == [1] and ds.attrs["stepStride"].tolist() == [2]
+        assert ds.attrs["nsteps"].tolist() == [4]
+        assert ds.attrs["storagetype"].tolist() == [storage]
+        assert ds.attrs["dimLengths"].tolist() == dim_lens
+        assert ds.attrs["binSchemes"].tolist() == sch
+        assert list(ds.dims) == [d[0] for d in ref["dims"]]
+        assert [[v.name, list(v.dims), v.nctype] for v in ds.vars.values()] == ref["vars"]
+
+    # --- 1-D
+    for typ, f, content in ((1, "bnd", "B"), (2, "ang", "A"), (3, "tor", "D")):
+        ds = cdf5.read(str(out / f"hist_{f}-1d.nc"))
+        k = bins[typ].shape[0]
+        check_header(ds, content, 1, 0, [k])
+        assert ds.vars["id"].data.ravel().tolist() == list(range(k))
+        np.testing.assert_array_equal(ds.vars["extrema"].data[:, 0], ext[typ])
+        fr = ds.vars["freq"].data
+        for r in range(k):
+            np.testing.assert_array_equal(ds.vars["mid"].data[r], mids(ext[typ][r]))
+            for si, t in enumerate(steps):
+                want = np.concatenate([np.bincount(bins[typ][r, s, :(t + 1) * step], minlength=nb)
+                                       for s, nb in enumerate(sch)])
+                np.testing.assert_array_equal(fr[r, si], want)
+    # --- 2-D
+    for f, tx, ty, content in (("bnd", 1, 1, "B/B"), ("ang", 2, 2, "A/A"), ("tor", 3, 3, "D/D"),
+                               ("ba", 1, 2, "B/A"), ("bd", 1, 3, "B/D"), ("ad", 2, 3, "A/D")):
+        ds = cdf5.read(str(out / f"hist_{f}-2d.nc"))
+        kx, ky = bins[tx].shape[0], bins[ty].shape[0]
+        check_header(ds, content, 2, 0 if tx == ty else 3, [kx, ky])
+        ids = ds.vars["id"].data
+        eids, _ = cdf5.read_entcontri(str(out / f"entcontri_{f}-2d.nc"))
+        assert np.array_equal(ids, eids)
+        fr = ds.vars["freq"].data
+        for r in range(0, ids.shape[0], max(1, ids.shape[0] // 7)):
+            a, b = ids[r]
+            np.testing.assert_array_equal(ds.vars["extrema"].data[r, 0], ext[tx][a])
+            np.testing.assert_array_equal(ds.vars["extrema"].data[r, 1], ext[ty][b])
+            # per scheme: the first DOF's mids, then the second's (binData2D)
+            m = sum((mids1(ext[tx][a], nb) + mids1(ext[ty][b], nb) for nb in sch), [])
+            np.testing.assert_array_equal(ds.vars["mid"].data[r], np.array(m))
+            for si, t in enumerate(steps):
+                want = []
+                for s, nb in enumerate(sch):
+                    x = bins[tx][a, s, :(t + 1) * step].astype(np.int64)
+                    y = bins[ty][b, s, :(t + 1) * step].astype(np.int64)
+                    want.append(np.bincount(x * nb + y, minlength=nb * nb))
+                np.testing.assert_array_equal(fr[r, si], np.concatenate(want))

@@ -182,3 +182,34 @@ def test_example1_sums_and_tree_from_reference_entropies(orc, ex1, ex1ent):
         got = sorted((inv[src[e]][0], inv[dst[e]][0], inv[src[e]][1], inv[dst[e]][1]) for e in tree)
         want = sorted((a, b, i, j) for a, b, i, j, _ in meta["trees"][str(step)])
         assert got == want, step
+
+
+# ------------------------------------------------ histogram dump (ex-2) --
+def hist_mids(mn, mx, schemes):
+    """binData1D's bin mids (src/Estimators.cpp:67-77): a running offset
+    from the minimum, half a bin width added.  The C++ driver writes the same
+    expression into hist_*.nc (host/stages.cpp, append_mids)."""
+    out = []
+    for nb in schemes:
+        w = (mx - mn) / nb
+        half = w / 2.0
+        off = mn
+        for _ in range(nb):
+            out.append(off + half)
+            off += w
+    return np.array(out)
+
+
+def test_hist_dump_golden_mids_and_counts():
+    g = np.load(os.path.join(GOLDEN, "hist_tor1d_ref.npz"))
+    hdr = json.load(open(os.path.join(GOLDEN, "hist_tor1d_ref.json")))
+    atts = {a[0]: a for a in hdr["atts"]}
+    schemes = atts["binSchemes"][2]
+    nsteps, first, stride = atts["nsteps"][2][0], atts["firstStep"][2][0], atts["stepStride"][2][0]
+    assert (first, stride) == (nsteps - 1, 1)       # the default: the last step only
+    for r in range(g["id"].shape[0]):
+        mn, mx = g["extrema"][r, 0, 0], g["extrema"][r, 0, 1]
+        np.testing.assert_array_equal(g["mid"][r], hist_mids(mn, mx, schemes))
+    # cumulative counts of the last step: every record counts the same frames
+    tot = g["freq"].sum(axis=2)
+    assert np.all(tot == tot[0, 0]) and tot[0, 0] > 0
