@@ -119,6 +119,7 @@ _SIGS = {
     "centre_gpu_discretize_vmkde": (C.c_int, [_vp, _vp, C.c_uint32, C.c_uint64, C.c_uint8,
                                               C.c_double, C.c_uint32, C.c_double, C.c_uint32,
                                               _vp, _vp, _vp]),
+    "centre_gpu_df_exp_eval": (C.c_int, [_vp, _vp, C.c_uint64, _vp]),
     "centre_gpu_discretize_gridkde": (C.c_int, [_vp, C.c_int, _vp, C.c_uint32, C.c_uint64,
                                                 C.c_uint32, C.c_double, _vp, _vp, _vp, _vp]),
     "centre_gpu_discretize_gridkde_dev": (C.c_int, [_vp, C.c_int, _vp, C.c_uint32, C.c_uint64,

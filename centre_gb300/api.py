@@ -135,6 +135,13 @@ class Context:
                                                         _ptr(minima), _ptr(nmin), _ptr(nbins)))
         return bins, minima, nmin, nbins
 
+    def df_exp_eval(self, y):
+        """The library's double-float e^y (y <= 0) for an array of doubles."""
+        y = _c(y, np.float64)
+        out = np.empty_like(y)
+        self.check(self.L.centre_gpu_df_exp_eval(self.h, _ptr(y), y.size, _ptr(out)))
+        return out
+
     def discretize_gridkde_dev(self, bat_type, data, ngrid, kappa, bins_out, minima_out,
                                nmin_out, nbins_out):
         """Device-pointer form of discretize_gridkde (torch CUDA tensors)."""

@@ -831,6 +831,22 @@ int centre_gpu_discretize_vmkde(centre_ctx *ctx, const float *data, uint32_t ndo
   return CENTRE_OK;
 }
 
+int centre_gpu_df_exp_eval(centre_ctx *ctx, const double *y, uint64_t n, double *out) {
+  if (!ctx || ((!y || !out) && n)) return set_error(ctx, CENTRE_E_ARG, "null argument");
+  if (n == 0) return CENTRE_OK;
+  cudaSetDevice(ctx->device);
+  int st = CENTRE_OK;
+  double *d = (double *)scratch(ctx, kSlotAux, sizeof(double) * 2 * n, &st);
+  if (!d) return st;
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(d, y, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                   ctx->stream));
+  CENTRE_TRY(launch_df_exp_eval(ctx, d, n, d + n));
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+  CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return CENTRE_OK;
+}
+
 int centre_gpu_discretize_gridkde_dev(centre_ctx *ctx, int bat_type, const float *data,
                                       uint32_t ndof, uint64_t nframes, uint32_t ngrid,
                                       double kappa, uint8_t *bins, double *minima,

@@ -191,6 +191,7 @@ int launch_gridkde(centre_ctx *ctx, int bat_type, const float *d_data, uint32_t 
                    uint64_t nframes, int ngrid, double kappa, uint8_t *d_bins, double *d_minima,
                    uint8_t *d_nmin, uint8_t *d_nbins, void *d_work);
 size_t gridkde_work_bytes(uint32_t ndof);
+int launch_df_exp_eval(centre_ctx *ctx, const double *d_y, uint64_t n, double *d_out);
 
 // pairs_tc.cu
 bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes);

@@ -22,9 +22,15 @@
 // GB300 mapping: one CTA of 4 warps per DOF.
 //  * torsions: lane l owns grid points l, l + 32, ...; each warp takes a
 //    quarter of the frames 32 at a time, every lane loading one frame
-//    (coalesced) and preparing it (cos a, sin a in FP64), then the 32 frames
-//    are broadcast by warp shuffles and each lane adds its grid points' terms
-//    (one FP64 exp per term; FP64 is the bound).
+//    (coalesced) and preparing its half-angle sine and cosine, then the 32
+//    frames are broadcast by warp shuffles and each lane adds its grid
+//    points' terms.  The terms run in double-float arithmetic on the FP32
+//    pipe (dfloat.cuh): kappa (cos t - 1) = -2 kappa sin^2(t/2) with
+//    sin((g - a)/2) from the half-angle products (no cancellation near
+//    t = 0), e^y by a table-driven double-float exp, double-float sums; the
+//    terms agree with FP64 to ~1e-12 relative.  A grid point whose
+//    double-float density is below 1e-25 (terms under the FP32 range) is
+//    summed again in FP64, so empty regions of the circle keep FP64 values.
 //  * bonds/angles: every thread takes its own frames and walks the grid
 //    outwards from the frame's nearest grid point with the Gaussian's
 //    multiplicative recurrence (z_{j+1} = z_j + s, s = step / h):
@@ -35,9 +41,11 @@
 //    steps).
 // The partial sums are combined in a fixed order, one thread finds the minima
 // and the CTA labels the DOF's frames.
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace centre {
 namespace {
@@ -155,30 +163,99 @@ gridkde_kernel(const float *__restrict__ data, uint64_t n, int ngrid, double kap
     }
   }
   if (kTorsion) {
+    __shared__ float dftab[2 * kDfExpTable];
+    if (tid < kDfExpTable) {
+      const double t = exp2((double)tid / kDfExpTable);
+      const float hi = __double2float_rn(t);
+      dftab[2 * tid] = hi;
+      dftab[2 * tid + 1] = __double2float_rn(t - (double)hi);
+    }
+    __syncthreads();
+    dfl sgh[kPerLane], cgh[kPerLane], dacc[kPerLane];
+#pragma unroll
+    for (int k = 0; k < kPerLane; ++k) {
+      const double h = 0.5 * kTwoPiG * (lane + 32 * k) / ngrid;   // half the grid angle
+      sgh[k] = df_from_double(sin(h));
+      cgh[k] = df_from_double(cos(h));
+      dacc[k] = df_make(0.0f, 0.0f);
+    }
+    const dfl m2k = df_from_double(-2.0 * kappa);
     const uint64_t per = (n + kGkWarps - 1) / kGkWarps;
     const uint64_t f0 = (uint64_t)warp * per, f1 = min(n, f0 + per);
     bool bad = false;
     for (uint64_t b = f0; b < f1; b += 32) {
       const uint64_t i = b + lane;
       const int cnt = (int)min((uint64_t)32, f1 - b);
-      double p = 0.0, q = 0.0;
+      dfl sa = df_make(0.0f, 0.0f), ca = df_make(1.0f, 0.0f);
       if (i < f1) {
         const float v = x[i];
         bad |= !isfinite(v);
-        sincos((double)v, &q, &p);   // p = cos a, q = sin a
+        double sh, ch;
+        sincos(0.5 * (double)v, &sh, &ch);
+        sa = df_from_double(sh);
+        ca = df_from_double(ch);
       }
       for (int f = 0; f < cnt; ++f) {
-        const double pf = __shfl_sync(0xffffffffu, p, f);
-        const double qf = __shfl_sync(0xffffffffu, q, f);
+        const dfl saf = df_make(__shfl_sync(0xffffffffu, sa.hi, f), __shfl_sync(0xffffffffu, sa.lo, f));
+        const dfl caf = df_make(__shfl_sync(0xffffffffu, ca.hi, f), __shfl_sync(0xffffffffu, ca.lo, f));
 #pragma unroll
-        for (int k = 0; k < kPerLane; ++k)
-          if (lane + 32 * k < ngrid) acc[k] += exp(kappa * (ga[k] * pf + gb[k] * qf - 1.0));
+        for (int k = 0; k < kPerLane; ++k) {
+          if (lane + 32 * k < ngrid) {
+            // sin((g - a)/2), then kappa (cos(g - a) - 1) = -2 kappa sin^2
+            const dfl sd = df_add(df_mul(sgh[k], caf), df_mul(cgh[k], df_make(-saf.hi, -saf.lo)));
+            const dfl y = df_mul(df_mul(sd, sd), m2k);
+            dacc[k] = df_add(dacc[k], df_exp_neg(y, dftab));
+          }
+        }
       }
     }
     if (bad) atomicOr(flag, kFlagDomain);
 #pragma unroll
     for (int k = 0; k < kPerLane; ++k)
-      if (lane + 32 * k < ngrid) part[warp][lane + 32 * k] = acc[k];
+      if (lane + 32 * k < ngrid) part[warp][lane + 32 * k] = df_value(dacc[k].hi, dacc[k].lo);
+    __syncthreads();
+    // grid points below the double-float range: FP64 sums (lanes own grid
+    // points as above; the other lanes idle through the frames)
+    bool tiny = false;
+#pragma unroll
+    for (int k = 0; k < kPerLane; ++k) {
+      const int j = lane + 32 * k;
+      if (j < ngrid) {
+        double t = 0.0;
+        for (int w = 0; w < kGkWarps; ++w) t += part[w][j];
+        tiny |= t < 1e-25;
+      }
+    }
+    if (__syncthreads_or(tiny)) {
+#pragma unroll
+      for (int k = 0; k < kPerLane; ++k) acc[k] = 0.0;
+      bool need[kPerLane];
+#pragma unroll
+      for (int k = 0; k < kPerLane; ++k) {
+        const int j = lane + 32 * k;
+        double t = 0.0;
+        if (j < ngrid)
+          for (int w = 0; w < kGkWarps; ++w) t += part[w][j];
+        need[k] = j < ngrid && t < 1e-25;
+      }
+      __syncthreads();
+      for (uint64_t b = f0; b < f1; b += 32) {
+        const uint64_t i = b + lane;
+        const int cnt = (int)min((uint64_t)32, f1 - b);
+        double p = 0.0, q = 0.0;
+        if (i < f1) sincos((double)x[i], &q, &p);   // p = cos a, q = sin a
+        for (int f = 0; f < cnt; ++f) {
+          const double pf = __shfl_sync(0xffffffffu, p, f);
+          const double qf = __shfl_sync(0xffffffffu, q, f);
+#pragma unroll
+          for (int k = 0; k < kPerLane; ++k)
+            if (need[k]) acc[k] += exp(kappa * (ga[k] * pf + gb[k] * qf - 1.0));
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kPerLane; ++k)
+        if (need[k]) part[warp][lane + 32 * k] = acc[k];
+    }
   } else {
     for (int j = 0; j < ngrid; ++j) gacc[j * kGkThreads + tid] = 0.0;
     if (!flat) {
@@ -264,7 +341,34 @@ gridkde_kernel(const float *__restrict__ data, uint64_t n, int ngrid, double kap
   }
 }
 
+// e^y of the double-float exponential for given doubles y (its test hook)
+__global__ void df_exp_eval_kernel(const double *__restrict__ y, uint64_t n,
+                                   double *__restrict__ out) {
+  __shared__ float tab[2 * kDfExpTable];
+  if (threadIdx.x < kDfExpTable) {
+    const double t = exp2((double)threadIdx.x / kDfExpTable);
+    const float hi = __double2float_rn(t);
+    tab[2 * threadIdx.x] = hi;
+    tab[2 * threadIdx.x + 1] = __double2float_rn(t - (double)hi);
+  }
+  __syncthreads();
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const dfl r = df_exp_neg(df_from_double(y[i]), tab);
+    out[i] = df_value(r.hi, r.lo);
+  }
+}
+
 }  // namespace
+
+int launch_df_exp_eval(centre_ctx *ctx, const double *d_y, uint64_t n, double *d_out) {
+  if (n == 0) return CENTRE_OK;
+  const unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, 1024);
+  df_exp_eval_kernel<<<grid, 256, 0, ctx->stream>>>(d_y, n, d_out);
+  ctx->launches += 1;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  return CENTRE_OK;
+}
 
 size_t gridkde_work_bytes(uint32_t ndof) { return sizeof(LinGrid) * (size_t)ndof; }
 

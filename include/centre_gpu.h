@@ -155,6 +155,12 @@ int centre_gpu_discretize_gridkde_dev(centre_ctx *ctx, int bat_type, const float
                                       double kappa, uint8_t *bins, double *minima,
                                       uint8_t *nmin, uint8_t *nbins);
 
+/* Diagnostics: the double-float e^y (y <= 0; ~48-bit, table-driven, on the
+ * FP32 pipe) that the grid KDE's torsion sums use, evaluated for host
+ * doubles y into host doubles out, so tests can bound its error against
+ * FP64.  No reference counterpart. */
+int centre_gpu_df_exp_eval(centre_ctx *ctx, const double *y, uint64_t n, double *out);
+
 /* ------------------------------------------------------------ entropy ---- */
 /* 1-D counts and entropies: binData1D (src/Estimators.cpp:56) + entropy1D
  * (:217) for every DOF, as EntropyCalculator::run1d (EntropyCalculator.cpp:

@@ -102,3 +102,24 @@ def test_gridkde_dev_matches_host(gpu):
         np.testing.assert_array_equal(m.cpu().numpy(), hm)
         np.testing.assert_array_equal(nm.cpu().numpy(), hn)
         np.testing.assert_array_equal(nb.cpu().numpy(), hnb)
+
+
+def test_df_exp_error_bound(gpu):
+    """The double-float e^y of the torsion sums (Tang's table-driven method on
+    FP32 pairs) against FP64 on [-70, 0] (where the low word is a normal
+    float): relative error below 5e-14 plus |y| * 4e-15 (y itself carries
+    ~48 bits as a double-float); FP32-level down to -87, exact 0 below."""
+    rng = np.random.default_rng(11)
+    y = np.concatenate([-70.0 * rng.random(200_000), -rng.random(50_000) * 1e-3,
+                        np.array([0.0, -1e-30, -0.5, -np.log(2) / 128]),
+                        -np.arange(0, 70, 0.25)])
+    got = gpu.df_exp_eval(y)
+    want = np.exp(y)
+    rel = np.abs(got - want) / want
+    bound = 5e-14 + 4e-15 * np.abs(y)
+    assert np.all(rel < bound), (rel.max(), y[np.argmax(rel / bound)])
+    # near the end of the FP32 range the low word turns subnormal: FP32-level
+    # accuracy there (such terms are summed again in FP64 when they dominate)
+    y2 = -70.0 - 17.0 * rng.random(10_000)
+    assert np.max(np.abs(gpu.df_exp_eval(y2) - np.exp(y2)) / np.exp(y2)) < 1e-6
+    assert np.all(gpu.df_exp_eval(np.array([-87.5, -100.0, -1e3])) == 0.0)
