@@ -29,8 +29,11 @@
 //    sin((g - a)/2) from the half-angle products (no cancellation near
 //    t = 0), e^y by a table-driven double-float exp, double-float sums; the
 //    terms agree with FP64 to ~1e-12 relative.  A grid point whose
-//    double-float density is below 1e-25 (terms under the FP32 range) is
-//    summed again in FP64, so empty regions of the circle keep FP64 values.
+//    double-float density is below kDfFloor is summed again in FP64: terms
+//    under the FP32 range (below e^-87, dropped) or with a subnormal low word
+//    (below e^-70) could otherwise matter there, so empty regions of the
+//    circle keep FP64 values (above the floor the dropped mass, at most
+//    N e^-70, stays below 4e-13 of the density for N up to 10^8).
 //  * bonds/angles: every thread takes its own frames and walks the grid
 //    outwards from the frame's nearest grid point with the Gaussian's
 //    multiplicative recurrence (z_{j+1} = z_j + s, s = step / h):
@@ -55,6 +58,7 @@ constexpr int kGkThreads = 128;
 constexpr int kGkWarps = kGkThreads / 32;
 constexpr int kMaxGrid = 128;
 constexpr int kPerLane = kMaxGrid / 32;
+constexpr double kDfFloor = 1e-10;   // double-float densities below: FP64 again
 
 // Per-DOF Gaussian grid of a bond/angle DOF: lo, grid step, 1/h; degenerate
 // (zero range or zero spread) DOFs get step 0 and a single bin.
@@ -223,7 +227,7 @@ gridkde_kernel(const float *__restrict__ data, uint64_t n, int ngrid, double kap
       if (j < ngrid) {
         double t = 0.0;
         for (int w = 0; w < kGkWarps; ++w) t += part[w][j];
-        tiny |= t < 1e-25;
+        tiny |= t < kDfFloor;
       }
     }
     if (__syncthreads_or(tiny)) {
@@ -236,7 +240,7 @@ gridkde_kernel(const float *__restrict__ data, uint64_t n, int ngrid, double kap
         double t = 0.0;
         if (j < ngrid)
           for (int w = 0; w < kGkWarps; ++w) t += part[w][j];
-        need[k] = j < ngrid && t < 1e-25;
+        need[k] = j < ngrid && t < kDfFloor;
       }
       __syncthreads();
       for (uint64_t b = f0; b < f1; b += 32) {

@@ -30,6 +30,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "dfloat.cuh"
 
 namespace centre {
 namespace {
@@ -99,35 +100,99 @@ double host_bessel_in(int n, double x) {
 }
 
 // Grid sums of one torsion: grad[g] and sec[g] as vonMises() returns them.
+// With a bandwidth h <= 700 the terms run in double-float arithmetic on the
+// FP32 pipe (dfloat.cuh): e^(h c) = e^h e^(h (c - 1)), the second factor by
+// the table-driven double-float exp (it is at most 1, so it stays in FP32
+// range), sums in double-float, and e^h applied once in FP64 at the end;
+// terms agree with FP64 to ~1e-12 relative.  A grid point whose scaled
+// weight sum is below kDfFloor (terms beyond the FP32 range could matter
+// there) is summed again in FP64, as is every grid point when h > 700.
+constexpr double kDfFloor = 1e-10;
+
 __global__ void __launch_bounds__(384)
 vmkde_grid_kernel(const float *__restrict__ data, uint64_t n, double h, double denom,
                   double *__restrict__ grad, double *__restrict__ sec) {
-  __shared__ double cs[kStageFrames], sn[kStageFrames];
+  __shared__ float4 fr[kStageFrames];       // cos a, sin a as double-floats
+  __shared__ float dftab[2 * kDfExpTable];
   const uint64_t d = blockIdx.x;
   const float *x = data + d * n;
   const int g = threadIdx.x;
   const double xg = g * kDegRad;
   const double cg = cos(xg), sg = sin(xg);
+  const bool use_df = h <= 700.0;
+  if (g < kDfExpTable) {
+    const double t = exp2((double)g / kDfExpTable);
+    const float hi = __double2float_rn(t);
+    dftab[2 * g] = hi;
+    dftab[2 * g + 1] = __double2float_rn(t - (double)hi);
+  }
   double G = 0.0, Sc = 0.0;
-  for (uint64_t f0 = 0; f0 < n; f0 += kStageFrames) {
-    const int cnt = (int)((n - f0) < (uint64_t)kStageFrames ? (n - f0) : (uint64_t)kStageFrames);
-    __syncthreads();
-    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
-      double s, c;
-      sincos((double)x[f0 + j], &s, &c);
-      cs[j] = c;
-      sn[j] = s;
-    }
-    __syncthreads();
-    if (g < kGrid) {
-      for (int j = 0; j < cnt; ++j) {
-        const double ca = cs[j], sa = sn[j];
-        const double c = cg * ca + sg * sa;   // cos(xg - a)
-        const double s = sg * ca - cg * sa;   // sin(xg - a)
-        const double e = exp(h * c);
-        G = G - s * e;
-        Sc = Sc + (h * (s * s) - c) * e;
+  bool need = g < kGrid;
+  if (use_df) {
+    const dfl cgd = df_from_double(cg), sgd = df_from_double(sg);
+    const dfl hd = df_from_double(h);
+    dfl Gd = df_make(0.0f, 0.0f), Sd = df_make(0.0f, 0.0f), Wd = df_make(0.0f, 0.0f);
+    for (uint64_t f0 = 0; f0 < n; f0 += kStageFrames) {
+      const int cnt = (int)((n - f0) < (uint64_t)kStageFrames ? (n - f0) : (uint64_t)kStageFrames);
+      __syncthreads();
+      for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+        double sa, ca;
+        sincos((double)x[f0 + j], &sa, &ca);
+        const dfl c2 = df_from_double(ca), s2 = df_from_double(sa);
+        fr[j] = make_float4(c2.hi, c2.lo, s2.hi, s2.lo);
       }
+      __syncthreads();
+      if (g < kGrid) {
+        for (int j = 0; j < cnt; ++j) {
+          const float4 q = fr[j];
+          const dfl ca = df_make(q.x, q.y), sa = df_make(q.z, q.w);
+          const dfl c = df_add(df_mul(cgd, ca), df_mul(sgd, sa));                  // cos(xg - a)
+          const dfl sn = df_add(df_mul(sgd, ca), df_mul(cgd, df_make(-sa.hi, -sa.lo)));  // sin
+          const dfl e = df_exp_neg(df_mul(hd, df_add(c, df_make(-1.0f, 0.0f))), dftab);
+          Gd = df_add(Gd, df_mul(df_make(-sn.hi, -sn.lo), e));
+          const dfl w = df_add(df_mul(hd, df_mul(sn, sn)), df_make(-c.hi, -c.lo));
+          Sd = df_add(Sd, df_mul(w, e));
+          Wd = df_add(Wd, e);
+        }
+      }
+    }
+    if (g < kGrid) {
+      const double eh = exp(h);
+      G = df_value(Gd.hi, Gd.lo) * eh;
+      Sc = df_value(Sd.hi, Sd.lo) * eh;
+      need = df_value(Wd.hi, Wd.lo) < kDfFloor;
+    }
+  }
+  __syncthreads();
+  if (__syncthreads_or(need)) {
+    // FP64 sums, frames staged as (cos a, sin a) doubles in the same buffer
+    double *cs = reinterpret_cast<double *>(fr);
+    double *sn = cs + kStageFrames;
+    double G2 = 0.0, S2 = 0.0;
+    for (uint64_t f0 = 0; f0 < n; f0 += kStageFrames) {
+      const int cnt = (int)((n - f0) < (uint64_t)kStageFrames ? (n - f0) : (uint64_t)kStageFrames);
+      __syncthreads();
+      for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+        double s, c;
+        sincos((double)x[f0 + j], &s, &c);
+        cs[j] = c;
+        sn[j] = s;
+      }
+      __syncthreads();
+      if (need) {
+        for (int j = 0; j < cnt; ++j) {
+          const double ca = cs[j], sa = sn[j];
+          const double c = cg * ca + sg * sa;   // cos(xg - a)
+          const double s = sg * ca - cg * sa;   // sin(xg - a)
+          const double e = exp(h * c);
+          G2 = G2 - s * e;
+          S2 = S2 + (h * (s * s) - c) * e;
+        }
+      }
+    }
+    if (need) {
+      G = G2;
+      Sc = S2;
     }
   }
   if (g < kGrid) {
