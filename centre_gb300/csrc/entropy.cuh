@@ -127,10 +127,13 @@ __device__ __forceinline__ U128 clnc_fixed(unsigned c) { return u128_from_double
 // Row-major upper-triangular pair (i, j), i < j, of index p among all pairs
 // of n items: a single-precision estimate of the row, corrected exactly with
 // integer arithmetic (no FP64 on the per-element path).
+// (Conversions go through 32-bit integers: 64-bit integer <-> float
+// conversions run on the FP64 pipe, which is scarce on this part.)
 __device__ __forceinline__ void tri_pair(uint64_t p, uint64_t n, uint32_t &i, uint32_t &j) {
-  const float nn = (float)n;
-  const float disc = (2.f * nn - 1.f) * (2.f * nn - 1.f) - 8.f * (float)p;
-  long long r = (long long)((2.f * nn - 1.f - sqrtf(fmaxf(disc, 0.f))) * 0.5f);
+  const float nn = (float)(uint32_t)n;
+  const float pf = __fmaf_rn((float)(uint32_t)(p >> 32), 4294967296.f, (float)(uint32_t)p);
+  const float disc = (2.f * nn - 1.f) * (2.f * nn - 1.f) - 8.f * pf;
+  long long r = (int)((2.f * nn - 1.f - sqrtf(fmaxf(disc, 0.f))) * 0.5f);
   if (r < 0) r = 0;
   if (r > (long long)n - 2) r = (long long)n - 2;
   auto start = [n](long long rr) { return (uint64_t)rr * n - (uint64_t)rr * (uint64_t)(rr + 1) / 2; };

@@ -172,30 +172,34 @@ __global__ void mst_init_kernel(uint32_t *comp, uint32_t V, uint64_t n) {
   if (i < n) comp[i] = (uint32_t)(i % V);
 }
 
+// One thread per pair, looping over the G graphs: the pair's DOFs and edge
+// rank are found once (no 64-bit division or conversion per graph) and its
+// G MI values are contiguous.
 template <int kPass>
 __global__ void mst_pick_kernel(const __grid_constant__ ScoreParams S, const uint8_t *__restrict__ types,
                                 const uint32_t *__restrict__ pairs, const double *__restrict__ mi,
                                 const uint32_t *__restrict__ comp, unsigned long long *bestkey,
                                 unsigned long long *bestedge) {
-  const uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (idx >= S.npairs * (uint64_t)S.G) return;
-  const uint64_t p = idx / S.G;
-  const int g = (int)(idx % S.G);
+  const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (p >= S.npairs) return;
   uint32_t i, j;
   pair_of(S, pairs, p, i, j);
-  const uint32_t *cg_ = comp + (uint64_t)g * S.ndof;
-  const uint32_t ci = cg_[i], cj = cg_[j];
-  if (ci == cj) return;
-  const unsigned long long key = order_key(mi[idx]);
-  unsigned long long *bk = bestkey + (uint64_t)g * S.ndof;
-  if (kPass == 0) {
-    if (key > bk[ci]) atomicMax(&bk[ci], key);
-    if (key > bk[cj]) atomicMax(&bk[cj], key);
-  } else {
-    unsigned long long *be = bestedge + (uint64_t)g * S.ndof;
-    const unsigned long long r = edge_rank(S, p, i, j, types);
-    if (key == bk[ci]) atomicMin(&be[ci], r);
-    if (key == bk[cj]) atomicMin(&be[cj], r);
+  const unsigned long long r = (kPass == 1) ? edge_rank(S, p, i, j, types) : 0ull;
+  const double *m = mi + p * S.G;
+  for (int g = 0; g < S.G; ++g) {
+    const uint32_t *cg_ = comp + (uint64_t)g * S.ndof;
+    const uint32_t ci = cg_[i], cj = cg_[j];
+    if (ci == cj) continue;
+    const unsigned long long key = order_key(m[g]);
+    unsigned long long *bk = bestkey + (uint64_t)g * S.ndof;
+    if (kPass == 0) {
+      if (key > bk[ci]) atomicMax(&bk[ci], key);
+      if (key > bk[cj]) atomicMax(&bk[cj], key);
+    } else {
+      unsigned long long *be = bestedge + (uint64_t)g * S.ndof;
+      if (key == bk[ci]) atomicMin(&be[ci], r);
+      if (key == bk[cj]) atomicMin(&be[cj], r);
+    }
   }
 }
 
@@ -207,21 +211,22 @@ __global__ void mst_hook_kernel(const __grid_constant__ ScoreParams S, const uin
                                 const unsigned long long *__restrict__ bestedge,
                                 unsigned long long *winpair, uint32_t *tree, uint32_t *ntree,
                                 uint32_t cap, unsigned *added) {
-  // pass A (grid over pairs): record the pair index of each winning rank
-  const uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (idx >= S.npairs * (uint64_t)S.G) return;
-  const uint64_t p = idx / S.G;
-  const int g = (int)(idx % S.G);
+  // pass A (one thread per pair, every graph): record the pair index of
+  // each winning rank
+  const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (p >= S.npairs) return;
   uint32_t i, j;
   pair_of(S, pairs, p, i, j);
-  const uint32_t *cg_ = comp + (uint64_t)g * S.ndof;
-  const uint32_t ci = cg_[i], cj = cg_[j];
-  if (ci == cj) return;
   const unsigned long long r = edge_rank(S, p, i, j, types);
-  const unsigned long long *be = bestedge + (uint64_t)g * S.ndof;
-  unsigned long long *wp = winpair + (uint64_t)g * S.ndof;
-  if (be[ci] == r) wp[ci] = p;
-  if (be[cj] == r) wp[cj] = p;
+  for (int g = 0; g < S.G; ++g) {
+    const uint32_t *cg_ = comp + (uint64_t)g * S.ndof;
+    const uint32_t ci = cg_[i], cj = cg_[j];
+    if (ci == cj) continue;
+    const unsigned long long *be = bestedge + (uint64_t)g * S.ndof;
+    unsigned long long *wp = winpair + (uint64_t)g * S.ndof;
+    if (be[ci] == r) wp[ci] = p;
+    if (be[cj] == r) wp[cj] = p;
+  }
 }
 
 __global__ void mst_link_kernel(const __grid_constant__ ScoreParams S, const uint32_t *__restrict__ pairs,
@@ -388,11 +393,11 @@ int launch_score_async(centre_ctx *ctx, const ScoreParams &S, const uint8_t *d_t
   while ((1u << (rounds - 1)) < S.ndof) ++rounds;
   for (int r = 0; r < rounds && PG > 0; ++r) {
     mst_reset_kernel<<<blocks(GV), TB, 0, ctx->stream>>>(bestkey, bestedge, GV);
-    mst_pick_kernel<0><<<blocks(PG), TB, 0, ctx->stream>>>(S, d_types, d_pairs, d_mi, comp,
-                                                           bestkey, bestedge);
-    mst_pick_kernel<1><<<blocks(PG), TB, 0, ctx->stream>>>(S, d_types, d_pairs, d_mi, comp,
-                                                           bestkey, bestedge);
-    mst_hook_kernel<<<blocks(PG), TB, 0, ctx->stream>>>(S, d_types, d_pairs, d_mi, comp, parent,
+    mst_pick_kernel<0><<<blocks(S.npairs), TB, 0, ctx->stream>>>(S, d_types, d_pairs, d_mi,
+                                                                 comp, bestkey, bestedge);
+    mst_pick_kernel<1><<<blocks(S.npairs), TB, 0, ctx->stream>>>(S, d_types, d_pairs, d_mi,
+                                                                 comp, bestkey, bestedge);
+    mst_hook_kernel<<<blocks(S.npairs), TB, 0, ctx->stream>>>(S, d_types, d_pairs, d_mi, comp, parent,
                                                         bestkey, bestedge, winpair, tree, ntree,
                                                         cap, added);
     mst_link_kernel<<<blocks(GV), TB, 0, ctx->stream>>>(S, d_pairs, comp, parent, bestedge,
@@ -471,11 +476,11 @@ int launch_score(centre_ctx *ctx, const ScoreParams &S, const uint8_t *d_types,
   for (uint32_t round = 0; round < 64 && PG > 0; ++round) {
     CENTRE_CUDA(ctx, cudaMemsetAsync(added, 0, sizeof(unsigned), ctx->stream));
     mst_reset_kernel<<<blocks(GV), TB, 0, ctx->stream>>>(bestkey, bestedge, GV);
-    mst_pick_kernel<0><<<blocks(PG), TB, 0, ctx->stream>>>(S, d_types, d_pairs, mi, comp, bestkey,
-                                                           bestedge);
-    mst_pick_kernel<1><<<blocks(PG), TB, 0, ctx->stream>>>(S, d_types, d_pairs, mi, comp, bestkey,
-                                                           bestedge);
-    mst_hook_kernel<<<blocks(PG), TB, 0, ctx->stream>>>(S, d_types, d_pairs, mi, comp, parent,
+    mst_pick_kernel<0><<<blocks(S.npairs), TB, 0, ctx->stream>>>(S, d_types, d_pairs, mi, comp,
+                                                                 bestkey, bestedge);
+    mst_pick_kernel<1><<<blocks(S.npairs), TB, 0, ctx->stream>>>(S, d_types, d_pairs, mi, comp,
+                                                                 bestkey, bestedge);
+    mst_hook_kernel<<<blocks(S.npairs), TB, 0, ctx->stream>>>(S, d_types, d_pairs, mi, comp, parent,
                                                         bestkey, bestedge, winpair, tree, ntree,
                                                         cap, added);
     mst_link_kernel<<<blocks(GV), TB, 0, ctx->stream>>>(S, d_pairs, comp, parent, bestedge,
