@@ -63,6 +63,15 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
   const bool hj = (type == 1 || type == 2);
   for (int b = tid; b < nb; b += blockDim.x)
     mids[b] = hj ? __dadd_rn(__dadd_rn(mn, __dmul_rn((double)b, w)), hw) : 0.0;
+  // the Jacobian factor of each bin and the log the L sum uses do not change
+  // with the step: evaluated once (FP64 transcendentals are the bound here)
+  __shared__ double jfs[256], ljs[256];
+  __syncthreads();
+  if (P.jacobian && hj)
+    for (int b = tid; b < nb; b += blockDim.x) {
+      jfs[b] = (type == 1) ? pow(mids[b], 2) : sin(mids[b]);
+      ljs[b] = log(type == 1 ? mids[b] * mids[b] : sin(mids[b]));
+    }
   const int nsum = P.nbins_sum;
   const int off = P.scheme_off[s];
   const uint64_t per = (uint64_t)P.nests * P.nschemes * P.nsteps;
@@ -118,7 +127,7 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
       double L = 0.0;
       if (P.jacobian && hj)
         for (int b = 0; b < nb; ++b)
-          if (cum[b]) L += (double)cum[b] * log(type == 1 ? mids[b] * mids[b] : sin(mids[b]));
+          if (cum[b]) L += (double)cum[b] * ljs[b];
       lsum[((uint64_t)dof * P.nschemes + s) * P.nsteps + t] = L;
     }
     // entropies: one warp per estimator
@@ -134,7 +143,7 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
           double pd = fq / w;
           if (pd > 0.0) {
             if (P.jacobian && hj) {
-              double jf = (type == 1) ? pow(mids[b], 2) : sin(mids[b]);
+              const double jf = jfs[b];
               pd = pd / jf;
               acc += jf * pd * log(pd);
             } else {
@@ -160,7 +169,7 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
           if (pd > 0.0) {
             double den = 1 - pow((1 - fq), nd);
             if (P.jacobian && hj) {
-              double jf = (type == 1) ? pow(mids[b], 2) : sin(mids[b]);
+              const double jf = jfs[b];
               pd = pd / jf;
               acc += jf * pd * log(pd) / den;
             } else {
@@ -188,7 +197,7 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
           double pd = fq / w;
           if (pd > 0.0) {
             if (P.jacobian && hj) {
-              double jf = (type == 1) ? pow(mids[b], 2) : sin(mids[b]);
+              const double jf = jfs[b];
               pd = pd / jf;
               acc += jf * pd * log(pd);
             } else {
