@@ -363,7 +363,9 @@ def run_ours(args):
         i, j = np.minimum(gp[:, 0], gp[:, 1]), np.maximum(gp[:, 0], gp[:, 1])
         idx = i * ndof - i * (i + 1) // 2 + (j - i - 1)
         s2g = s2.reshape(npairs, NSTEPS)[torch.from_numpy(idx).to(dev)].cpu().numpy()
-        rel = np.abs(s2g - s2o) / np.maximum(np.abs(s2o), 1e-13)
+        err = np.abs(s2g - s2o)
+        big = np.abs(s2o) > 1e-6
+        rel = err[big] / np.abs(s2o[big]) if big.any() else np.zeros(1)
         out["cpu_baseline"] = {
             "value": cpu_pairs_per_s(w, t_d, t_1, t_p), "unit": UNIT, "cores": cores,
             "kind": "port",
@@ -371,7 +373,13 @@ def run_ours(args):
                       f"discretised on {cores} host threads, extrapolated to {npairs} pairs; "
                       "MST excluded",
             "gpu_vs_oracle_s2": {"pairs": int(len(idx)) * NSTEPS,
-                                 "max_rel_error": float(rel.max())}}
+                                 # relative error where |S2| > 1e-6; absolute error
+                                 # everywhere (joint entropies with Jacobian terms can
+                                 # sit within rounding of zero)
+                                 "max_rel_error": float(rel.max()),
+                                 "max_abs_error": float(err.max()),
+                                 "within_test_tolerance": bool(
+                                     np.all(err <= 1e-9 * np.abs(s2o) + 1e-13))}}
     ctx.close()
     if rank == 0:
         print(json.dumps(out))
