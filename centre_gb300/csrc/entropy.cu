@@ -860,7 +860,10 @@ int launch_entropy1d(centre_ctx *ctx, const EntParams &P, uint32_t ndof, const u
 
 // Shared-memory budget of the histograms (the 128-bit c ln c table and the
 // kernel's static data take the rest of the 227 KB).
-static constexpr size_t kHistBudget = 184 * 1024;
+#ifndef CENTRE_HIST_BUDGET_KB
+#define CENTRE_HIST_BUDGET_KB 184
+#endif
+static constexpr size_t kHistBudget = CENTRE_HIST_BUDGET_KB * 1024;
 
 int pair_tile_for(int nb) {
   // pairs whose nb*nb uint32 histograms fit the shared-memory budget
