@@ -39,10 +39,31 @@ namespace {
 constexpr double kPi = 3.141592653589793;      // src/Constants.h:92
 constexpr double kTwoPi = 6.283185307179586;   // src/Constants.h:94
 constexpr double kDx = 5.0e-9;                 // src/configcentre.h:22
-constexpr int kThreads = 512;
+#ifndef CENTRE_DISC_THREADS
+#define CENTRE_DISC_THREADS 512
+#endif
+#ifndef CENTRE_DISC_MIN_BLOCKS
+#define CENTRE_DISC_MIN_BLOCKS 3     // resident CTAs per SM (registers <= 40)
+#endif
+constexpr int kThreads = CENTRE_DISC_THREADS;
+static_assert(kThreads >= 256 && kThreads <= 1024 && kThreads % 32 == 0,
+              "the table build gives each thread at most one entry of 256");
 constexpr int kMaxFit = 180;                   // src/Real2Int.cpp:269
-constexpr int kMaxCluster = 8;
-constexpr size_t kStageBytes = 104 * 1024;     // shared-memory slice per CTA
+// cluster size cap and shared-memory slice per CTA (build-time knobs; a DOF
+// whose slice exceeds the budget at the largest cluster is read twice, the
+// second time from L2, instead of staged).  Every CTA of a cluster repeats
+// the per-DOF serial phases (cluster reduction, range, thresholds, table), so
+// few CTAs per DOF and more resident CTAs per SM win: on 2994 DOFs x 100,000
+// frames, clusters of 2 unstaged with 3 CTAs of 512 threads per SM took
+// 1.17 ms against 2.63 ms for staged clusters of 4 at 2 CTAs per SM.
+#ifndef CENTRE_DISC_MAX_CLUSTER
+#define CENTRE_DISC_MAX_CLUSTER 2
+#endif
+#ifndef CENTRE_DISC_STAGE_KB
+#define CENTRE_DISC_STAGE_KB 104
+#endif
+constexpr int kMaxCluster = CENTRE_DISC_MAX_CLUSTER;
+constexpr size_t kStageBytes = CENTRE_DISC_STAGE_KB * 1024;
 constexpr int kLut = 256;                      // binning lookup-table entries
 
 struct DiscParams {
@@ -185,7 +206,7 @@ struct DofState {
   int bad;
 };
 
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, CENTRE_DISC_MIN_BLOCKS)
 discretize_kernel(const float *__restrict__ data, uint8_t *__restrict__ bins,
                   double *__restrict__ extremes, const __grid_constant__ DiscParams P,
                   int *__restrict__ flag) {

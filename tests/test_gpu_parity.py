@@ -46,7 +46,7 @@ def test_discretize_golden_fixture(gpu, golden):
                 np.testing.assert_allclose(ext[:, 2], want[:, 2], rtol=1e-12, err_msg=key)
 
 
-@pytest.mark.parametrize("nframes", [50_000, 20_001, 1_003, 37, 150_000])
+@pytest.mark.parametrize("nframes", [50_000, 20_001, 1_003, 37, 150_000, 300_001])
 def test_discretize_synthetic_vs_oracle(gpu, orc, nframes):
     tr = chain_trajectory(9, nframes, seed=nframes)
     for typ, blk in tr.blocks():
