@@ -243,6 +243,15 @@ constexpr int kRedBatch = 4;    // cells per lane per batch in the moment reduct
 // kernel keeps the one-cell-at-a-time reduction and fewer registers: its
 // autotuned tiles favour more resident CTAs.
 constexpr int kHistMinBlocks = CENTRE_HIST_MIN_BLOCKS;
+#ifndef CENTRE_HIST_INTERLEAVE
+#define CENTRE_HIST_INTERLEAVE 1
+#endif
+// 4 x 4 tiles of the single-trajectory kernel use interleaved histograms
+constexpr bool kHistInterleave = CENTRE_HIST_INTERLEAVE != 0;
+#ifndef CENTRE_HIST_PREFETCH
+#define CENTRE_HIST_PREFETCH 1
+#endif
+constexpr bool kHistPrefetch = CENTRE_HIST_PREFETCH != 0;
 
 __device__ __forceinline__ void red_shared_inc(uint32_t addr) {
   asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr) : "memory");
@@ -298,14 +307,33 @@ __device__ void decode_all_pairs_tile(uint64_t id, uint64_t ntile, uint32_t ndof
 // Count all frames of one tile and emit its moments (or counts) per step.
 // `hist` is zeroed on entry and left zeroed.  Returns non-zero if a bin was
 // out of range.  All threads of the CTA call it.
-template <int R, int C, bool kCounts, bool kBatchedRed>
+//
+// kIlv (interleaved histograms, NP = R*C dividing 32): cell k of pair P is
+// word k*NP + P instead of P*nb*nb + k, and lane l counts the pair rotated
+// by its slot s = l mod NP (row (r + s/C) mod R, column (c + s%C) mod C at
+// unrolled step (r, c)), so the NP lanes of a slot group update NP different
+// pairs: for NP = 16 a warp's increments fall on bank P + 16 (k mod 2), at
+// most two per bank, where 32 lanes updating one pair at random cells load
+// the busiest bank ~3.3 times (shared-memory wavefronts bound this kernel).
+// The loaded words are rotated in registers, so the loads stay coalesced.
+// The moment reduction then sweeps the whole tile with the CTA: a lane's
+// words all belong to pair l mod NP.
+template <int R, int C, bool kCounts, bool kBatchedRed, bool kIlv = false>
 __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_t *cols_s,
                          const uint64_t *out_s, unsigned *hist, const U128 *tab,
                          const unsigned long long *tab64, const double *__restrict__ gtab) {
   constexpr int NP = R * C;
+  static_assert(!kIlv || (32 % NP == 0 && NP > 1), "interleaving needs NP | 32");
+  constexpr bool kPrefetch = kIlv && kHistPrefetch;
   const int tid = threadIdx.x;
   const int nb = J.nb, nb2 = nb * nb;
   const uint64_t n = J.nframes;
+  // lane slot of the interleaved layout: row and column rotation
+  const int slot = kIlv ? (int)(threadIdx.x & 31) % NP : 0;
+  const int rrot = slot / C, crot = slot % C;
+  // byte strides of one row bin / one column bin in the histogram words
+  const uint32_t rstride = kIlv ? 4u * (uint32_t)nb * NP : 4u * (uint32_t)nb;
+  const uint32_t cstride = kIlv ? 4u * NP : 4u;
   const uint8_t *bins = J.bins;
   const uint32_t hist_s = (uint32_t)__cvta_generic_to_shared(hist);
   // DOF rows as 32-bit word offsets (row starts are 4-byte aligned when the
@@ -327,13 +355,29 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       rw0[r] = (uint32_t)((((uint64_t)rows_s[r] * J.nschemes + J.scheme) * n) >> 2);
-      rconst[r] = hist_s + 4u * (uint32_t)(r * C * nb2);
+      rconst[r] = kIlv ? hist_s + 4u * (uint32_t)(((r + rrot) % R) * C)
+                       : hist_s + 4u * (uint32_t)(r * C * nb2);
     }
 #pragma unroll
     for (int c = 0; c < C; ++c) {
       cw0[c] = (uint32_t)((((uint64_t)cols_s[c] * J.nschemes + J.scheme) * n) >> 2);
-      cconst[c] = 4u * (uint32_t)(c * nb2);
+      cconst[c] = kIlv ? 4u * (uint32_t)((c + crot) % C) : 4u * (uint32_t)(c * nb2);
     }
+  };
+  // x rotated by k places (y[i] = x[(i + k) mod N]) with selects: no
+  // dynamically indexed registers
+  auto rotate = [](auto &x, int k) {
+    constexpr int N = sizeof(x) / sizeof(x[0]);
+    uint32_t y[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      uint32_t v = x[i];
+#pragma unroll
+      for (int j = 1; j < N; ++j) v = (k == j) ? x[(i + j) % N] : v;
+      y[i] = v;
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) x[i] = y[i];
   };
   if (!kBatchedRed) setup();
   for (int t = 0; t < J.nsteps; ++t) {
@@ -356,39 +400,64 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
         bad = 1;
         return;
       }
+      if (kIlv) {
 #pragma unroll
-      for (int r = 0; r < R; ++r)
+        for (int r = 0; r < R; ++r)
 #pragma unroll
-        for (int c = 0; c < C; ++c) red_shared_inc(rconst[r] + a[r] * nb4 + cconst[c] + 4u * b[c]);
+          for (int c = 0; c < C; ++c)
+            red_shared_inc(hist_s + 4u * (uint32_t)(r * C + c) + a[r] * rstride + b[c] * cstride);
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+          for (int c = 0; c < C; ++c) red_shared_inc(rconst[r] + a[r] * nb4 + cconst[c] + 4u * b[c]);
+      }
     };
     if (word) {
       const uint64_t g0 = (f0 + 3) >> 2, g1 = f1 >> 2;   // whole 4-frame groups
       for (uint64_t f = f0 + tid; f < min(f1, g0 << 2); f += blockDim.x) one_frame(f);
       for (uint64_t f = max(f0, g1 << 2) + tid; f < f1; f += blockDim.x) one_frame(f);
+      // kPrefetch: the next group's words are loaded before this group's
+      // increments (the red.shared asm keeps later loads behind it)
+      uint32_t rn[R], cn[C];
+      auto load_group = [&](uint64_t g, uint32_t (&x)[R], uint32_t (&y)[C]) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) x[r] = __ldg(bw + rw0[r] + (uint32_t)g);
+#pragma unroll
+        for (int c = 0; c < C; ++c) y[c] = __ldg(bw + cw0[c] + (uint32_t)g);
+      };
+      if (kPrefetch && g0 + tid < g1) load_group(g0 + tid, rn, cn);
       for (uint64_t g = g0 + tid; g < g1; g += blockDim.x) {
         uint32_t rw[R], cw[C];
+        if (kPrefetch) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) rw[r] = rn[r];
+#pragma unroll
+          for (int c = 0; c < C; ++c) cw[c] = cn[c];
+          if (g + blockDim.x < g1) load_group(g + blockDim.x, rn, cn);
+        } else {
+          load_group(g, rw, cw);
+        }
         uint32_t v = 0;
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          rw[r] = __ldg(bw + rw0[r] + (uint32_t)g);
-          v |= __vcmpgeu4(rw[r], lim);
-        }
+        for (int r = 0; r < R; ++r) v |= __vcmpgeu4(rw[r], lim);
 #pragma unroll
-        for (int c = 0; c < C; ++c) {
-          cw[c] = __ldg(bw + cw0[c] + (uint32_t)g);
-          v |= __vcmpgeu4(cw[c], lim);
-        }
+        for (int c = 0; c < C; ++c) v |= __vcmpgeu4(cw[c], lim);
         if (v) {
           bad = 1;
           continue;
+        }
+        if (kIlv) {
+          rotate(rw, rrot);
+          rotate(cw, crot);
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           uint32_t ro[R], co[C];
 #pragma unroll
-          for (int r = 0; r < R; ++r) ro[r] = rconst[r] + ((rw[r] >> (8 * q)) & 255u) * nb4;
+          for (int r = 0; r < R; ++r) ro[r] = rconst[r] + ((rw[r] >> (8 * q)) & 255u) * rstride;
 #pragma unroll
-          for (int c = 0; c < C; ++c) co[c] = cconst[c] + ((cw[c] >> (8 * q)) & 255u) * 4u;
+          for (int c = 0; c < C; ++c) co[c] = cconst[c] + ((cw[c] >> (8 * q)) & 255u) * cstride;
 #pragma unroll
           for (int r = 0; r < R; ++r)
 #pragma unroll
@@ -404,7 +473,75 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
         const uint64_t o = out_s[q];
         if (o == ~0ull) continue;
         unsigned *dst = J.counts + (o * J.nsteps + t) * (uint64_t)nb2;
-        for (int i = tid; i < nb2; i += blockDim.x) dst[i] = hist[q * nb2 + i];
+        for (int i = tid; i < nb2; i += blockDim.x)
+          dst[i] = kIlv ? hist[i * NP + q] : hist[q * nb2 + i];
+      }
+    } else if constexpr (kIlv) {
+      // the CTA sweeps all NP * nb2 words; lane l only meets pair l mod NP.
+      // Sums are exact (integer), so the order does not matter.
+      constexpr int kW = 16;   // warps of the 512-thread CTA
+      __shared__ U128 wacc_s[kW][NP];
+      __shared__ unsigned wnz_s[kW][NP];
+      const int warp = tid >> 5, lane = tid & 31;
+      const int tot = NP * nb2, stride = (int)blockDim.x;
+      U128 acc;
+      acc.lo = acc.hi = 0ull;
+      unsigned cz = 0;
+      // warp-uniform trip count (the warp votes below need every lane)
+      for (int k0 = warp * 32; k0 < tot; k0 += stride * kRedBatch) {
+        unsigned c[kRedBatch];
+        U128 v[kRedBatch];
+        bool big = false;
+#pragma unroll
+        for (int u = 0; u < kRedBatch; ++u) {
+          const int k = k0 + u * stride + lane;
+          c[u] = (k < tot) ? hist[k] : 0u;
+          big |= c[u] >= (unsigned)kTab64;
+          v[u].lo = tab64[min(c[u], (unsigned)kTab64 - 1u)];
+          v[u].hi = 0ull;
+        }
+        if (__any_sync(0xffffffffu, big)) {
+          double fv[kRedBatch];
+#pragma unroll
+          for (int u = 0; u < kRedBatch; ++u)
+            if (c[u] >= (unsigned)kTabHist)
+              fv[u] = __ldg(gtab + min(c[u], (unsigned)kTabGlobal - 1u));
+#pragma unroll
+          for (int u = 0; u < kRedBatch; ++u)
+            if (c[u] >= (unsigned)kTab64)
+              v[u] = (c[u] < (unsigned)kTabHist)    ? tab[c[u]]
+                     : (c[u] < (unsigned)kTabGlobal) ? u128_from_double(fv[u])
+                                                      : clnc_far_u128(gtab, c[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < kRedBatch; ++u) {
+          acc = u128_add(acc, v[u]);
+          cz += (c[u] != 0);
+        }
+      }
+      // lanes l, l + NP, ... hold the same pair
+#pragma unroll
+      for (int off = 16; off >= NP; off >>= 1) {
+        acc = u128_add(acc, u128_shfl_xor(acc, off));
+        cz += __shfl_xor_sync(0xffffffffu, cz, off);
+      }
+      if (lane < NP) {
+        wacc_s[warp][lane] = acc;
+        wnz_s[warp][lane] = cz;
+      }
+      __syncthreads();
+      if (tid < NP) {
+        const uint64_t o = out_s[tid];
+        if (o != ~0ull) {
+          U128 s = wacc_s[0][tid];
+          unsigned z = wnz_s[0][tid];
+          for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            s = u128_add(s, wacc_s[w][tid]);
+            z += wnz_s[w][tid];
+          }
+          J.sclnc[o * J.nsteps + t] = s;
+          J.nnz[o * J.nsteps + t] = z;
+        }
       }
     } else {
       // one warp per pair: exact sum of c ln c and non-empty cells
@@ -480,8 +617,8 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
   return bad;
 }
 
-template <int R, int C, bool kCounts>
-__global__ void __launch_bounds__(512, kHistMinBlocks)
+template <int R, int C, bool kCounts, int kMinBlocks = kHistMinBlocks>
+__global__ void __launch_bounds__(512, kMinBlocks)
 pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__ tasks,
                   const __grid_constant__ PairParams P, const double *__restrict__ gtab,
                   U128 *__restrict__ sclnc, unsigned *__restrict__ nnz,
@@ -522,8 +659,8 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
   J.sclnc = sclnc;
   J.nnz = nnz;
   J.counts = counts;
-  const int bad =
-      hist_tile<R, C, kCounts, true>(J, rows_s, cols_s, out_s, hist, tab, tab64, gtab);
+  const int bad = hist_tile<R, C, kCounts, true, kHistInterleave && R == 4 && C == 4>(
+      J, rows_s, cols_s, out_s, hist, tab, tab64, gtab);
   if (bad && tid == 0) atomicOr(flag, kFlagBinRange);
 }
 
@@ -871,12 +1008,46 @@ int pair_tile_for(int nb) {
   return (int)std::min<size_t>(16, kHistBudget / per);
 }
 
+template <int R, int C, int kMinB>
+static int launch_hist_mb(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
+                          uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
+                          unsigned *d_counts, size_t smem) {
+  if (d_counts) {
+    CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, true, kMinB>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pairs_hist_kernel<R, C, true, kMinB><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
+        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+  } else {
+    CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, false, kMinB>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pairs_hist_kernel<R, C, false, kMinB><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
+        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+  }
+  return CENTRE_OK;
+}
+
 template <int R, int C>
 static int launch_hist(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
                        uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
                        unsigned *d_counts) {
   const size_t smem =
       (((size_t)R * C * P.nb * P.nb * 4 + 15) & ~size_t(15)) + 16 * kTabHist + 8 * kTab64;
+  if (R == 4 && C == 4 && kHistPrefetch) {
+    // the prefetching 4 x 4 kernel is built twice: capped at 64 registers
+    // for two resident CTAs, and uncapped (~120 registers) for histograms
+    // so large that one CTA fills an SM's shared memory anyway (50 bins:
+    // 218 vs 233 ms for the 2994-DOF chain)
+    int per_sm = 0;
+    CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, false, 2>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CENTRE_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                         &per_sm, pairs_hist_kernel<R, C, false, 2>, 512, smem));
+    if (per_sm < 2)
+      return launch_hist_mb<R, C, 1>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts,
+                                     smem);
+    return launch_hist_mb<R, C, 2>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts,
+                                   smem);
+  }
   if (d_counts) {
     CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, true>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
