@@ -42,14 +42,14 @@ NSTEPS = 10
 
 
 # DRAM bytes per pair of one all-pairs count launch (100,000 frames, 50 bins,
-# 10 steps), from an ncu capture of 176,121 pairs: 61.4 MB read + 14.6 MB
+# 10 steps), from an ncu capture of 176,121 pairs: 61.3 MB read + 14.3 MB
 # written.
-PAIR_TRAFFIC_PER_PAIR = 76.0e6 / 176121
+PAIR_TRAFFIC_PER_PAIR = 75.6e6 / 176121
 # Shared-memory wavefronts per histogram increment of the same capture
-# (1.784e9 wavefronts for 1.761e10 increments: the atomics, 2.02 per warp
+# (1.704e9 wavefronts for 1.761e10 increments: the atomics, 2.0 per warp
 # instruction with the interleaved histograms, plus the per-step moment
 # reductions); the data pipe retires one wavefront per SM cycle.
-HIST_WAVEFRONTS_PER_INCREMENT = 1.784e9 / 1.761e10
+HIST_WAVEFRONTS_PER_INCREMENT = 1.704e9 / 1.761e10
 SM_COUNT = 152
 
 
@@ -310,7 +310,7 @@ def run_ours(args):
                      "traffic": PAIR_TRAFFIC_PER_PAIR * npairs,
                      "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu "
                                      "capture of the same kernel on the 594-DOF chain (100,000 "
-                                     "frames, 50 bins, 10 steps): 76.0 MB for 176,121 pairs, "
+                                     "frames, 50 bins, 10 steps): 75.6 MB for 176,121 pairs, "
                                      "scaled by pairs to this launch",
                      "note": f"2*N*B^2 flops per pair (B={NBINS} real bins); fp8 peak = 2 x "
                              f"{src} bf16 {bf16:.0f} TF/s"},
