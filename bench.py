@@ -323,7 +323,7 @@ def run_ours(args):
     if args.compare_atomic:
         # both count forms on the same data (the metric compares them): the
         # one the timed steps did not use runs one more (warm, timed) step
-        uses_tc = form == 2 or (form == 0 and NBINS <= 16)
+        uses_tc = form == 2 or (form == 0 and NBINS > 217)
         other = 1 if uses_tc else 2
         try:
             step(other)
@@ -344,7 +344,7 @@ def run_ours(args):
     clocks = clk.summary()
     if clocks:
         out["clocks"] = clocks
-    if args.form == "atomic" or (args.form == "auto" and NBINS > 16):
+    if args.form == "atomic" or (args.form == "auto" and NBINS <= 217):
         # the histogram form's own bound: the shared-memory data pipe
         mhz = (clocks or {}).get("sm_mhz") or 2070.0
         incr = float(used) * npairs / (pair_ms / 1e3)

@@ -716,7 +716,7 @@ pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nit
 
 // ----------------------------------------------------------------------------
 // Joint counts for bin counts whose histograms do not fit shared memory
-// (more than 214 bins): each CTA owns one nb x nb histogram in global
+// (more than 217 bins): each CTA owns one nb x nb histogram in global
 // memory (L2-resident) and counts a pair's frames into it with global
 // atomics, one pair at a time.  At every step it emits the pair's moments
 // (or copies the cumulative counts), then clears the histogram.  Reads of

@@ -198,8 +198,12 @@ int launch_df_exp_eval(centre_ctx *ctx, const double *d_y, uint64_t n, double *d
 
 // pairs_tc.cu
 bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes);
-// largest bin count at which AUTO prefers the tensor-core contraction
-constexpr int kTcAutoMaxBins = 16;
+// largest bin count at which AUTO prefers the tensor-core contraction over
+// a shared-memory histogram that fits (none: with interleaved histograms the
+// histogram form is faster at every bin count it covers, e.g. 134 vs 159 ms
+// at 16 bins for the 2994-DOF chain); AUTO takes the contraction only where
+// the histograms do not fit shared memory
+constexpr int kTcAutoMaxBins = 0;
 int launch_pairs_tc(centre_ctx *ctx, const PairParams &P, const double *d_tab, U128 *d_sclnc,
                     unsigned *d_nnz);
 
