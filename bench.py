@@ -312,8 +312,12 @@ def run_ours(args):
                                      "capture of the same kernel on the 594-DOF chain (100,000 "
                                      "frames, 50 bins, 10 steps): 75.6 MB for 176,121 pairs, "
                                      "scaled by pairs to this launch",
-                     "note": f"2*N*B^2 flops per pair (B={NBINS} real bins); fp8 peak = 2 x "
-                             f"{src} bf16 {bf16:.0f} TF/s"},
+                     "note": f"2*N*B^2 flops per pair (B={NBINS} real bins): the dense one-hot "
+                             f"contraction's work; fp8 peak = 2 x {src} bf16 {bf16:.0f} TF/s. "
+                             "The timed launches are the form AUTO selects (the shared-memory "
+                             "histogram up to 217 bins: one increment per pair-frame instead of "
+                             "B^2 multiply-adds), so frac > 1 means the launch beats the "
+                             "contraction's ceiling; its own bound is smem_roofline"},
         "discretize_roofline": {"bound": "hbm", "achieved": disc_bytes / (disc_ms / 1e3) / 1e9,
                                 "peak": hbm, "unit": "GB/s",
                                 "frac": disc_bytes / (disc_ms / 1e3) / 1e9 / hbm,
