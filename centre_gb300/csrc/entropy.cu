@@ -317,13 +317,17 @@ __device__ void decode_all_pairs_tile(uint64_t id, uint64_t ntile, uint32_t ndof
 // the busiest bank ~3.3 times (shared-memory wavefronts bound this kernel).
 // The loaded words are rotated in registers, so the loads stay coalesced.
 // The moment reduction then sweeps the whole tile with the CTA: a lane's
-// words all belong to pair l mod NP.
+// words all belong to pair l mod NP (it needs the 64-bit table of the
+// batched reduction and 512 threads: 16 warps combine through shared memory).
+// With kIlv the next 4-frame group's words are also loaded before the
+// current group's increments (kHistPrefetch).
 template <int R, int C, bool kCounts, bool kBatchedRed, bool kIlv = false>
 __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_t *cols_s,
                          const uint64_t *out_s, unsigned *hist, const U128 *tab,
                          const unsigned long long *tab64, const double *__restrict__ gtab) {
   constexpr int NP = R * C;
   static_assert(!kIlv || (32 % NP == 0 && NP > 1), "interleaving needs NP | 32");
+  static_assert(!kIlv || kBatchedRed, "the interleaved reduction reads the 64-bit table");
   constexpr bool kPrefetch = kIlv && kHistPrefetch;
   const int tid = threadIdx.x;
   const int nb = J.nb, nb2 = nb * nb;
@@ -343,8 +347,6 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
   const uint32_t lim = 0x01010101u * (uint32_t)nb;
   const bool word = (n & 3) == 0;
   int bad = 0;
-
-
 
   // row/column word offsets and histogram addresses; with the batched
   // reduction they are recomputed every step so that none of them is live
