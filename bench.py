@@ -762,7 +762,7 @@ def run_screen(args):
     step trains the network on exact MI of 200,000 random pairs over the
     first 20 % of frames, keeps 64 partners per DOF, computes their exact
     joint entropies over all frames and runs MIE sums and MIST.  The plain
-    all-pairs MIST of the same data is timed once beside it and is the judge
+    all-pairs MIST of the same data is timed once beside it and is the yardstick
     of the total-entropy error."""
     import torch
     from centre_gb300.api import Context, make_params, make_screen_params
@@ -810,7 +810,7 @@ def run_screen(args):
         pairs, w, losses = ctx.screen_dev(p, sp, types, bins, ext)
         return mist(pairs), pairs.shape[0], losses
 
-    # the judge: plain all-pairs MIST, timed once after one warm-up
+    # the yardstick: plain all-pairs MIST, timed once after one warm-up
     t0 = time.perf_counter()
     full = mist(None)
     torch.cuda.synchronize(dev)

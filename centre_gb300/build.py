@@ -4,7 +4,7 @@ command-line tool centre_gpu on top of it.
 Each translation unit under csrc/ is compiled in parallel with nvcc and the
 objects are linked into centre_gb300/libcentre_gpu.so (no torch involved; the
 C ABI is declared in include/centre_gpu.h).  The host sources under host/
-(input file, NetCDF files, the three pipeline stages, the driver) are
+(input file, NetCDF files, the three pipeline stages, the command-line main) are
 compiled with the host C++ compiler and linked into centre_gb300/centre_gpu,
 which finds the library next to itself.
 
@@ -86,7 +86,7 @@ def _compile_host(src: str) -> str:
 
 
 def build_tool(jobs: int | None = None) -> str:
-    """centre_gpu: the input-file driver (host/), linked against the library."""
+    """centre_gpu: the input-file tool (host/), linked against the library."""
     srcs = sorted(f for f in os.listdir(HOST) if f.endswith(".cpp"))
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, len(srcs))) as ex:
         objs = list(ex.map(_compile_host, srcs))

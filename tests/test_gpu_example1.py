@@ -159,7 +159,7 @@ def test_driver_reproduces_reference_outputs(gpu, ex, tmp_path):
         mi = sorted(float(r.split(",")[4]) for r in lines[1:])
         np.testing.assert_allclose(mi, sorted(x[4] for x in meta["trees"][str(step)]),
                                    atol=0.5e-6 + 1e-9)
-    # the driver's own entropy-contribution files hold the reference's values
+    # the command-line tool's own entropy-contribution files hold the reference's values
     for f, _ in ONED:
         ids, c = cdf5.read_entcontri(str(out / f"entcontri_{f.replace('_', '-')}.nc"))
         assert np.array_equal(ids[:, 0], e[f + "_ids"][:, 0])

@@ -1,6 +1,6 @@
 """The learned pair screen on the GPU: its training kernels' gradients
 against the CPU oracle of the network, the shape of what it selects, and
-what it gains over the exact all-pairs method (the fallback and the judge):
+what it gains over the exact all-pairs method (the fallback and the yardstick):
 far fewer exact pairs at a total MIST entropy within 0.5 %."""
 import numpy as np
 import pytest
