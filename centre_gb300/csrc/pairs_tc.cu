@@ -125,6 +125,10 @@ struct SlotInfo {
 struct Smem {
   uint64_t full[kStages];
   uint64_t empty[kStages];
+  // per stage: the producer warps of the stage have cleared their previous
+  // chunk's bytes (needed when the stage moves to another tile, where the
+  // warps' DOF slots cover other rows)
+  uint64_t cleared[kStages];
   uint64_t accfull;
   uint64_t accempty;
   uint64_t drain;
@@ -475,6 +479,7 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&S.full[s], 32 * kPerStage);
       mbar_init(&S.empty[s], 1);
+      mbar_init(&S.cleared[s], kPerStage);
     }
     mbar_init(&S.accfull, 1);
     mbar_init(&S.accempty, kEpilogue);
@@ -570,6 +575,11 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
     uint32_t edgemask = 0;       // slots whose DOF is cut by the tile's edge
     // slot table of tile ti: lane i describes this warp's slot i
     auto set_tile = [&](uint64_t ti) {
+      // every lane has finished reading the previous tile's slot table
+      // (mark_set, load_lane_bins) before any lane overwrites its entry: a
+      // lane still marking the last chunk of the old tile would otherwise
+      // combine the old edge mask with the new slot geometry
+      __syncwarp();
       StageMeta m;
       tile_geometry(P, P.tiles[ti], m);
       const int slot = h + lane * kPerStage;
@@ -600,6 +610,8 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
       nvalid = (int)(cur.f1 - cur.f0);
       load_lane_bins(P, sl, nmine, nvalid, cur.f0, lane, pb);
     }
+    uint64_t marked = ~0ull;     // tile of the chunk this warp last marked
+    uint32_t cph = 0;            // phase of S.cleared[p]
     while (cur.valid) {
       // wait until the MMA has consumed this stage's previous chunk
       int go = 1;
@@ -611,7 +623,24 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
         mark_clear(addr);
       }
       __syncwarp();
+      if (used && cur.ti != marked) {
+        // The stage moves to another tile, where the other warps of this
+        // stage own rows this warp may have marked (and the reverse): every
+        // warp of the stage clears its previous chunk before any sets the
+        // new one.  All warps of a stage walk the same chunks, so they all
+        // take this branch together.
+        int ok = 1;
+        if (lane == 0) {
+          mbar_arrive(&S.cleared[p]);
+          ok = wait_bar(S, &S.cleared[p], cph, flag) ? 1 : 0;
+        }
+        cph ^= 1u;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) break;
+        __syncwarp();
+      }
       mark_set(P, sl, nmine, edgemask, nvalid, sink, lane, pb, addr, flag);
+      marked = cur.ti;
       fence_proxy_async();
       mbar_arrive(&S.full[p]);
       // fetch this warp's next chunk

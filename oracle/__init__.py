@@ -41,10 +41,14 @@ def build(with_ref: bool = True) -> None:
     """Compile liboracle.so (and the reference shim when the reference
     sources are present)."""
     subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
-    refroot = os.environ.get("CENTRE_REFERENCE_ROOT", "/root/reference")
-    if with_ref and os.path.isdir(os.path.join(refroot, "src")):
-        subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REFROOT={refroot}"],
-                       check=True)
+    if with_ref:
+        # the recipe builds the shim only where the reference checkout exists
+        # ($CENTRE_REFERENCE_ROOT, else the Makefile's REFROOT)
+        cmd = ["make", "-s", "-C", _HERE, "ref-if-present"]
+        refroot = os.environ.get("CENTRE_REFERENCE_ROOT")
+        if refroot:
+            cmd.append(f"REFROOT={refroot}")
+        subprocess.run(cmd, check=True)
 
 
 def ref_available() -> bool:

@@ -25,10 +25,9 @@ def orc():
 @pytest.fixture(scope="session")
 def ref():
     import oracle
-    refroot = os.environ.get("CENTRE_REFERENCE_ROOT", "/root/reference")
-    if not os.path.isdir(os.path.join(refroot, "src")):
-        pytest.skip("reference sources not present (only in the development checkout)")
     oracle.build(with_ref=True)
+    if not oracle.ref_available():
+        pytest.skip("reference sources not present (only in the development checkout)")
     return oracle.Reference()
 
 

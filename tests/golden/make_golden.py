@@ -1,9 +1,9 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
-Run in a checkout that has the reference sources (shaileshp51/centre) at
-$CENTRE_REFERENCE_ROOT (default /root/reference):
+Run where the reference sources (shaileshp51/centre) are checked out, with
+CENTRE_REFERENCE_ROOT naming that checkout:
 
-    python tests/golden/make_golden.py
+    CENTRE_REFERENCE_ROOT=<checkout> python tests/golden/make_golden.py
 
 It builds oracle/_ref/libcentre_ref.so from the reference's own numeric
 sources (oracle/Makefile), runs the reference functions on seeded inputs, and
@@ -45,7 +45,7 @@ sys.path.insert(0, ROOT)
 import oracle  # noqa: E402
 from centre_gb300 import cdf5  # noqa: E402
 
-REF = os.environ.get("CENTRE_REFERENCE_ROOT", "/root/reference")
+REF = os.environ.get("CENTRE_REFERENCE_ROOT", "")
 
 
 def dof_inputs(seed=7, n=4000):
@@ -217,6 +217,8 @@ def make_hist():
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(os.path.join(REF, "src")):
+        sys.exit("set CENTRE_REFERENCE_ROOT to the reference checkout")
     if sys.argv[1:] == ["example1"]:
         make_example1()
         sys.exit(0)

@@ -380,6 +380,38 @@ def test_tc_counts_identical_to_atomic(gpu, orc, natoms, nframes, nsteps, nb):
         assert np.array_equal(s_at, s_tc)
 
 
+@pytest.mark.parametrize("natoms,nframes,nsteps,nb", [
+    (200, 20_000, 4, 50), (200, 12_000, 3, 16), (120, 10_000, 2, 30)])
+def test_tc_counts_many_tiles_per_cta(gpu, orc, natoms, nframes, nsteps, nb):
+    """Thousands of 128 x 256 tiles for 152 persistent CTAs: every CTA walks
+    many tiles, and its producer warps move their stages from tile to tile
+    (the 594-DOF chain at 50 bins gives about 13,600 tiles).  The moments
+    must equal the shared-memory histogram's bit for bit on every run, and a
+    sample of pairs must equal the oracle's counts."""
+    tr = chain_trajectory(natoms, nframes, seed=natoms + nb, coupling="block8")
+    bins, ext, types = stack_blocks(tr, gpu, [nb])
+    pa = make_params(nframes, nsteps, [nb], [0, 1], True, counts_form=1)
+    pt = make_params(nframes, nsteps, [nb], [0, 1], True, counts_form=2)
+    ca, za = gpu.pair_moments(pa, bins)
+    for run in range(3):
+        ct, zt = gpu.pair_moments(pt, bins)
+        bad = np.nonzero(np.any(ct != ca, axis=(1, 2)) | np.any(zt != za, axis=1))[0]
+        assert len(bad) == 0, f"run {run}: {len(bad)} pairs differ, first {bad[:5]}"
+    ndof = len(bins)
+    rng = np.random.default_rng(nb)
+    for _ in range(12):
+        i, j = sorted(rng.choice(ndof, 2, replace=False))
+        q = i * ndof - i * (i + 1) // 2 + (j - i - 1)
+        f = orc.bin2d(bins[i, 0], bins[j, 0], nsteps, [nb]).reshape(nsteps, -1).astype(np.float64)
+        x = np.where(f > 1, f * np.log(np.where(f > 0, f, 1)), 0).sum(axis=1)
+        assert np.array_equal(zt[q], (f > 0).sum(axis=1)), (i, j)
+        xt = ct[q, :, 1].astype(np.float64) * 2.0 ** 12 + ct[q, :, 0].astype(np.float64) * 2.0 ** -52
+        np.testing.assert_allclose(xt, x, rtol=1e-12)
+    s_at = gpu.entropy2d(pa, types, bins, ext)
+    s_tc = gpu.entropy2d(pt, types, bins, ext)
+    assert np.array_equal(s_at, s_tc)
+
+
 # ----------------------------------------------------- von Mises KDE ----
 def _kde_compare(gb, gm, gf, ob, omins, of, x):
     """Bins equal except frames within rounding of a minimum; minima agree."""
