@@ -100,6 +100,8 @@ extern "C" int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entrop
     if (S.ndof < 2 || S.nframes < p->nsteps || S.nframes > kMaxFrames || !S.types || !S.bins ||
         !S.extremes || !S.s1 || !S.s2 || !S.mie_sums)
       return set_error(ctx, CENTRE_E_ARG, "bad trajectory in batch");
+    if ((uint64_t)S.ndof * p->nschemes * S.nframes >= kMaxHistBinBytes)
+      return set_error(ctx, CENTRE_E_ARG, "bin matrix of 16 GiB or more in batch");
   }
   const int G = p->nestimators * p->nschemes * p->nsteps;
   if (G > 256) return set_error(ctx, CENTRE_E_UNSUPPORTED, "estimators*schemes*steps must be <= 256");
@@ -357,7 +359,9 @@ extern "C" int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entrop
   CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   int flag = 0;
   CENTRE_CUDA(ctx, cudaMemcpy(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
-  if (flag & kFlagBinRange) return set_error(ctx, CENTRE_E_BINRANGE, "bin index >= bin count");
+  if (flag_status(flag) != CENTRE_OK)
+    return set_error(ctx, flag_status(flag), (flag & kFlagBinRange) ? "bin index >= bin count"
+                                                                    : "device error flag set");
   for (uint32_t k = 0; k < nsys; ++k) {
     const double *h = reinterpret_cast<const double *>(C.h_stage) + (size_t)k * G * CENTRE_SUMS_COLS * 2;
     memcpy(sys[k].mie_sums, h, sizeof(double) * G * CENTRE_SUMS_COLS);

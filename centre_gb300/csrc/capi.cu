@@ -121,13 +121,16 @@ int read_flag(centre_ctx *ctx) {
                                    ctx->stream));
   CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   const int f = *ctx->h_flag;
-  if (f & kFlagDomain)
-    return set_error(ctx, CENTRE_E_ARG,
-                     "input outside the reference's domain (bonds >= 0, angles in [0, pi], "
-                     "torsions in [0, 2pi), finite)");
-  if (f & kFlagBinRange) return set_error(ctx, CENTRE_E_BINRANGE, "bin index >= bin count");
-  if (f & kFlagTimeout) return set_error(ctx, CENTRE_E_TIMEOUT, "device wait limit reached");
-  return CENTRE_OK;
+  switch (flag_status(f)) {
+    case CENTRE_OK: return CENTRE_OK;
+    case CENTRE_E_ARG:
+      return set_error(ctx, CENTRE_E_ARG,
+                       "input outside the reference's domain (bonds >= 0, angles in [0, pi], "
+                       "torsions in [0, 2pi), finite)");
+    case CENTRE_E_BINRANGE: return set_error(ctx, CENTRE_E_BINRANGE, "bin index >= bin count");
+    case CENTRE_E_TIMEOUT: return set_error(ctx, CENTRE_E_TIMEOUT, "device wait limit reached");
+    default: return set_error(ctx, CENTRE_E_CUDA, "unknown device error flag");
+  }
 }
 
 // Tasks for an explicit pair list: pairs grouped by first DOF, up to `width`
@@ -277,12 +280,13 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
       P.nb = nb;
       P.nsteps = E.nsteps;
       const int form = p->counts_form;
-      // AUTO takes the tensor-core contraction at its smallest bin count
-      // (16: measured 158 ms against 176 ms for the histogram on all pairs
-      // of 2994 DOFs x 100,000 frames) and where histograms do not fit
-      // shared memory; otherwise the shared-memory histogram, which
-      // outruns the contraction as B^2 multiply-adds per frame and pair
-      // grow against its one increment (20 bins: 233 ms against 150 ms).
+      // AUTO takes the tensor-core contraction only where the histograms
+      // do not fit shared memory (more than 217 bins; kTcAutoMaxBins is 0).
+      // Everywhere else the shared-memory histogram wins: it does one
+      // increment per frame and pair where the contraction does B^2
+      // multiply-adds (all pairs of 2994 DOFs x 100,000 frames at 16 bins:
+      // histogram 134 ms, contraction 159 ms; at 50 bins 218 ms against
+      // 1,150 ms and more).
       const bool use_tc =
           all && tc_supported(ctx, nb, E.nframes) &&
           (form == CENTRE_COUNTS_TC ||

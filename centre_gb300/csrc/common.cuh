@@ -101,6 +101,20 @@ enum : int {
   kFlagDomain = 4,
 };
 
+// The status a device error flag maps to (every entry point uses this
+// mapping, so the same input gives the same status everywhere).
+inline int flag_status(int f) {
+  if (f & kFlagDomain) return CENTRE_E_ARG;
+  if (f & kFlagBinRange) return CENTRE_E_BINRANGE;
+  if (f & kFlagTimeout) return CENTRE_E_TIMEOUT;
+  return f ? CENTRE_E_CUDA : CENTRE_OK;
+}
+
+// The shared-memory histogram kernels address bin rows with 32-bit word
+// offsets: a bin matrix (DOFs x schemes x frames bytes) must stay below
+// 16 GiB for them.
+constexpr uint64_t kMaxHistBinBytes = 1ull << 34;
+
 // Order-preserving map of a double onto uint64 (larger double -> larger key).
 __host__ __device__ inline uint64_t order_key(double v) {
   union {

@@ -77,7 +77,9 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
   const uint64_t per = (uint64_t)P.nests * P.nschemes * P.nsteps;
 
   const int warp = tid >> 5, nwarps = blockDim.x >> 5;
-  const bool word = ((n & 3) == 0) && ((((uint64_t)dof * P.nschemes + s) * n & 3) == 0);
+  // 32-bit loads need every row start 4-byte aligned: the frame count and
+  // the caller's bins pointer (an offset view may not be)
+  const bool word = ((n & 3) == 0) && ((reinterpret_cast<uintptr_t>(bins) & 3) == 0);
   const uint32_t lim = 0x01010101u * (uint32_t)nb;
   for (int t = 0; t < P.nsteps; ++t) {
     for (int b = tid; b < 8 * 256; b += blockDim.x) whist[b] = 0;
@@ -345,7 +347,9 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
   const uint32_t *bw = reinterpret_cast<const uint32_t *>(bins);
   const uint32_t nb4 = 4u * (uint32_t)nb;
   const uint32_t lim = 0x01010101u * (uint32_t)nb;
-  const bool word = (n & 3) == 0;
+  // 32-bit loads need every row start 4-byte aligned: the frame count and
+  // the caller's bins pointer (an offset view may not be)
+  const bool word = ((n & 3) == 0) && ((reinterpret_cast<uintptr_t>(bins) & 3) == 0);
   int bad = 0;
 
   // row/column word offsets and histogram addresses; with the batched
@@ -1118,6 +1122,8 @@ int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_
                         uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
                         unsigned *d_counts) {
   if (ntasks == 0) return CENTRE_OK;
+  if ((uint64_t)P.ndof * P.nschemes * P.nframes >= kMaxHistBinBytes)
+    return set_error(ctx, CENTRE_E_ARG, "bin matrix of 16 GiB or more (histogram counts)");
   KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
   int rc;
   if (P.all_pairs) {

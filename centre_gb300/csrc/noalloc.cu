@@ -1,11 +1,10 @@
 // noalloc.cu -- 2-D joint entropies of all pairs without allocating memory.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA stream is
-// being captured into a graph (allocation is not a capturable operation),
-// plug-ins living inside an application whose memory manager owns every
-// device byte and forbids foreign allocations, and latency-critical loops
-// where an allocation could stall on a device-wide synchronisation.  For
-// them centre_gpu_entropy2d_static() computes what centre_gpu_entropy2d_dev()
+// Some callers cannot call cudaMalloc: plug-ins living inside an application
+// whose memory manager owns every device byte and forbids foreign
+// allocations, and latency-critical loops where an allocation could stall on
+// a device-wide synchronisation.  For them centre_gpu_entropy2d_static()
+// computes what centre_gpu_entropy2d_dev()
 // computes for the all-pairs case, with every piece of scratch memory taken
 // from one file-scope device array of fixed size (kStaticScratchBytes, 16
 // MiB) instead of the context's allocator.  The caller passes its inputs and
@@ -88,7 +87,8 @@ extern "C" int centre_gpu_entropy2d_static(const centre_entropy_params *p, uint3
   E.kde = p->kde ? 1 : 0;
   int off = 0;
   for (int s = 0; s < p->nschemes; ++s) {
-    if (p->bin_schemes[s] == 0 || pair_tile_for(p->bin_schemes[s]) < 1) return CENTRE_E_UNSUPPORTED;
+    if (p->bin_schemes[s] == 0) return CENTRE_E_ARG;
+    if (pair_tile_for(p->bin_schemes[s]) < 1) return CENTRE_E_UNSUPPORTED;
     E.schemes[s] = p->bin_schemes[s];
     E.scheme_off[s] = off;
     off += p->bin_schemes[s];
@@ -172,7 +172,5 @@ extern "C" int centre_gpu_entropy2d_static(const centre_entropy_params *p, uint3
   if (cudaMemcpyAsync(&h_flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return CENTRE_E_CUDA;
-  if (h_flag & kFlagBinRange) return CENTRE_E_BINRANGE;
-  if (h_flag) return CENTRE_E_CUDA;
-  return CENTRE_OK;
+  return flag_status(h_flag);
 }

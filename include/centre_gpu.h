@@ -193,9 +193,10 @@ int centre_gpu_entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p,
  * memory: no context is needed, all scratch space comes from one fixed
  * device array of 16 MiB inside the library.  No counterpart in the
  * reference, which allocates host memory per pair.  It serves callers that
- * must not call cudaMalloc: code running while its stream is captured into a
- * CUDA graph, plug-ins whose host application owns all device memory, and
- * loops where an allocation could stall on a device synchronisation.
+ * must not call cudaMalloc: plug-ins whose host application owns every byte
+ * of device memory through its own pool and forbids foreign allocations, and
+ * loops that must not stall on the device-wide synchronisation an
+ * allocation can cause.
  *   - Device pointers, enqueued on `cuda_stream`; returns after the stream
  *     has finished the call (it reads back an error flag).
  *   - ML and Miller-Madow estimators, shared-memory histogram counts only

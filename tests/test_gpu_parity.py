@@ -326,6 +326,34 @@ def test_example1_on_gpu(gpu):
             assert abs(mi - want) <= 0.5e-6 + 1e-9
 
 
+def test_entropies_from_unaligned_bins_view(gpu):
+    """A bins pointer that is not 4-byte aligned (an offset view into a
+    larger device buffer) takes the byte-load path and gives the same 1-D and
+    2-D entropies as an aligned copy."""
+    import torch
+    tr = chain_trajectory(10, 8_000, seed=3)
+    bins, ext, types = stack_blocks(tr, gpu, [30])
+    p = make_params(8_000, 4, [30], [0, 1], True)
+    want1 = gpu.entropy1d(p, types, bins, ext)
+    want2 = gpu.entropy2d(p, types, bins, ext)
+    dev = torch.device("cuda", 0)
+    raw = torch.zeros(bins.size + 3, dtype=torch.uint8, device=dev)
+    d_types = torch.from_numpy(types).to(dev)
+    d_ext = torch.from_numpy(ext).to(dev)
+    ndof = len(types)
+    for off in (1, 2, 3):
+        view = raw[off:off + bins.size].view(bins.shape)
+        view.copy_(torch.from_numpy(bins))
+        assert view.data_ptr() % 4 == off % 4
+        s1 = torch.empty((ndof, 2, 1, 4), dtype=torch.float64, device=dev)
+        s2 = torch.empty((ndof * (ndof - 1) // 2, 2, 1, 4), dtype=torch.float64, device=dev)
+        gpu.entropy1d_dev(p, d_types, view, d_ext, s1)
+        gpu.entropy2d_dev(p, d_types, view, d_ext, s2)
+        torch.cuda.synchronize()
+        assert np.array_equal(s1.cpu().numpy(), want1), off
+        assert np.array_equal(s2.cpu().numpy(), want2), off
+
+
 # ------------------------------------------------- size-independent checks --
 def test_full_size_properties(gpu):
     """At the 1000-atom shape: counts cover every frame of every step,

@@ -1,9 +1,9 @@
 """centre_gpu_entropy2d_static: the all-pairs joint entropies computed without
 any memory allocation by the library (its scratch is a fixed device array).
 
-It exists for callers that may not call cudaMalloc -- code running while its
-stream is captured into a CUDA graph, plug-ins whose host application owns all
-device memory, loops that must not stall on an allocation.  The test calls it
+It exists for callers that may not call cudaMalloc -- plug-ins whose host
+application owns all device memory through its own pool, loops that must not
+stall on the device synchronisation an allocation can cause.  The test calls it
 through the C ABI twice in a row (the second call runs on the array the first
 one left behind) and compares each result with the allocating entry point,
 centre_gpu_entropy2d, within the parity tolerance used everywhere else.  This
@@ -72,3 +72,23 @@ def test_static_scratch_entry_rejects_oversized_problems(gpu):
     rc = L.centre_gpu_entropy2d_static(C.byref(p), 5000, ptr, ptr, ptr, ptr,
                                        C.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == -1
+
+
+def test_static_scratch_entry_status_codes_match_allocating_entry(gpu):
+    """The same invalid input gives the same status from both entry points:
+    a bin scheme of zero bins is an argument error (CENTRE_E_ARG)."""
+    import torch
+    from centre_gb300.api import CentreError
+    L = _lib.load()
+    p = make_params(4_000, 2, [30], [0], True)
+    p.bin_schemes[0] = 0
+    bins = np.zeros((3, 1, 4_000), np.uint8)
+    ext = np.tile(np.array([0.0, 1.0, 0.5, 0.0]), (3, 1))
+    types = np.array([1, 2, 3], np.uint8)
+    with pytest.raises(CentreError) as e:
+        gpu.entropy2d(p, types, bins, ext)
+    dummy = torch.zeros(16, dtype=torch.float64, device="cuda")
+    ptr = C.c_void_p(dummy.data_ptr())
+    rc = L.centre_gpu_entropy2d_static(C.byref(p), 3, ptr, ptr, ptr, ptr,
+                                       C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == e.value.status == -1
