@@ -138,7 +138,7 @@ _SIGS = {
     "centre_gpu_counts2d": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp,
                                       C.c_uint64, _vp, _vp]),
     "centre_gpu_pair_moments": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp,
-                                          C.c_int, _vp, _vp]),
+                                          C.c_int, _vp, _vp, _vp]),
     "centre_gpu_score": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp, _vp,
                                    C.c_uint64, _vp, _vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     "centre_gpu_score_dev": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp, _vp,

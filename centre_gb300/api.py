@@ -192,16 +192,19 @@ class Context:
         return freq
 
     def pair_moments(self, params: EntropyParams, bins, scheme=0):
-        """Integer moments of every pair i<j: (clnc [npairs][nsteps][2] uint64
-        as (low, high) words of sum c ln c * 2^52, nnz [npairs][nsteps])."""
+        """Integer moments of every pair i<j: (clnc [npairs][nsteps] uint64,
+        the sum over cells of round(c ln c * 2^scale); nnz [npairs][nsteps],
+        the non-empty cells; scale)."""
         bins = _c(bins, np.uint8)
         ndof = bins.shape[0]
         npairs = ndof * (ndof - 1) // 2
-        clnc = np.zeros((npairs, params.nsteps, 2), np.uint64)
+        clnc = np.zeros((npairs, params.nsteps), np.uint64)
         nnz = np.zeros((npairs, params.nsteps), np.uint32)
+        scale = C.c_int(0)
         self.check(self.L.centre_gpu_pair_moments(self.h, C.byref(params), ndof, _ptr(bins),
-                                                  int(scheme), _ptr(clnc), _ptr(nnz)))
-        return clnc, nnz
+                                                  int(scheme), _ptr(clnc), _ptr(nnz),
+                                                  C.byref(scale)))
+        return clnc, nnz, scale.value
 
     def score(self, params: EntropyParams, types, s1, s2, pairs=None, build_tree=True,
               want_mi=True, mi_out=None):

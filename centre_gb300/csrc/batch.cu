@@ -14,6 +14,7 @@
 // candidates on a sample of the real work list (autotuning), once per
 // (bins, steps, schemes) combination per context.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -106,6 +107,15 @@ extern "C" int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entrop
   const int G = p->nestimators * p->nschemes * p->nsteps;
   if (G > 256) return set_error(ctx, CENTRE_E_UNSUPPORTED, "estimators*schemes*steps must be <= 256");
   BatchState &bs = state_of(ctx);
+  // one moment scale for every trajectory: the one of the longest (the
+  // table it needs is built here, before any capture)
+  uint64_t nmax = 0;
+  for (uint32_t k = 0; k < nsys; ++k)
+    nmax = std::max<uint64_t>(nmax, sys[k].nframes / p->nsteps * p->nsteps);
+  const int fscale = moment_scale(nmax);
+  int tst = CENTRE_OK;
+  const unsigned long long *d_fix = fix_table(ctx, fscale, &tst);
+  if (!d_fix) return tst;
 
   // ---- per-trajectory parameters and scratch layout ----------------------
   std::vector<EntParams> E(nsys);
@@ -133,6 +143,8 @@ extern "C" int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entrop
     }
     e.nbins_sum = off;
     for (int q = 0; q < p->nestimators; ++q) e.ests[q] = p->estimators[q];
+    e.fix_scale = fscale;
+    e.fix_inv = std::ldexp(1.0, -fscale);
     const uint64_t npairs = (uint64_t)S.ndof * (S.ndof - 1) / 2;
     ScoreParams &sp = SP[k];
     memset(&sp, 0, sizeof(sp));
@@ -154,7 +166,7 @@ extern "C" int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entrop
     off_l[k] = total;
     total += align256(sizeof(double) * S.ndof * p->nschemes * p->nsteps);
     off_m[k] = total;
-    total += align256(sizeof(U128) * npairs * p->nsteps);
+    total += align256(sizeof(unsigned long long) * npairs * p->nsteps);
     off_z[k] = total;
     total += align256(sizeof(unsigned) * npairs * p->nsteps);
     off_w[k] = total;
@@ -186,7 +198,7 @@ extern "C" int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entrop
       b.ndof = sys[k].ndof;
       b.ntile = (sys[k].ndof + tile - 1) / tile;
       b.item_begin = items;
-      b.sclnc = reinterpret_cast<U128 *>(base + off_m[k]);
+      b.sclnc = reinterpret_cast<unsigned long long *>(base + off_m[k]);
       b.nnz = reinterpret_cast<unsigned *>(base + off_z[k]);
       items += b.ntile * (b.ntile + 1) / 2;
     }
@@ -227,11 +239,11 @@ extern "C" int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entrop
         B.nschemes = p->nschemes;
         B.scheme = 0;
         B.nb = p->bin_schemes[0];
+        B.fix_scale = fscale;
         CENTRE_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
         CENTRE_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
         CENTRE_TRY(launch_pairs_hist_batch(ctx, d_sys, (int)nsys, sample, B, tile, threads,
-                                           (int)std::min<uint64_t>(grid, sample),
-                                           (const double *)ctx->d_clnc));
+                                           (int)std::min<uint64_t>(grid, sample), d_fix));
         CENTRE_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
         CENTRE_CUDA(ctx, cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -304,14 +316,15 @@ extern "C" int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entrop
         B.nschemes = p->nschemes;
         B.scheme = s;
         B.nb = p->bin_schemes[s];
+        B.fix_scale = fscale;
         const int grid = (int)std::min<uint64_t>(items, (uint64_t)ctx->sm_count * best.blocks_per_sm);
         rc = launch_pairs_hist_batch(ctx, d_sys, (int)nsys, items, B, best.tile, best.threads,
-                                     grid, (const double *)ctx->d_clnc);
+                                     grid, d_fix);
         for (uint32_t k = 0; k < nsys && rc == CENTRE_OK; ++k) {
           const uint64_t npairs = (uint64_t)sys[k].ndof * (sys[k].ndof - 1) / 2;
           rc = launch_finalize2d_into(ctx, E[k], s, sys[k].ndof, sys[k].extremes,
                                       reinterpret_cast<double *>(base + off_l[k]),
-                                      reinterpret_cast<U128 *>(base + off_m[k]),
+                                      reinterpret_cast<unsigned long long *>(base + off_m[k]),
                                       reinterpret_cast<unsigned *>(base + off_z[k]), npairs,
                                       reinterpret_cast<double *>(base + off_w[k]), sys[k].s2);
         }

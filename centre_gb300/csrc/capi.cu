@@ -1,5 +1,6 @@
 // capi.cu -- the C ABI of the library (declared in include/centre_gpu.h).
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
@@ -113,6 +114,8 @@ int validate_params(centre_ctx *ctx, const centre_entropy_params *p, EntParams *
     if (p->estimators[e] > 3) return set_error(ctx, CENTRE_E_ARG, "unknown estimator");
     E->ests[e] = p->estimators[e];
   }
+  E->fix_scale = moment_scale(E->step_size * E->nsteps);
+  E->fix_inv = std::ldexp(1.0, -E->fix_scale);
   return CENTRE_OK;
 }
 
@@ -191,8 +194,8 @@ int counts_chunk(centre_ctx *ctx, const EntParams &E, int scheme, uint32_t ndof,
     P.scheme = scheme;
     P.nb = nb;
     P.nsteps = E.nsteps;
-    CENTRE_TRY(launch_pairs_global(ctx, P, d_pl, 0, p1 - p0, (const double *)ctx->d_clnc,
-                                   nullptr, nullptr, d_counts));
+    CENTRE_TRY(launch_pairs_global(ctx, P, d_pl, 0, p1 - p0, nullptr, nullptr, nullptr,
+                                   d_counts));
     CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return CENTRE_OK;
   }
@@ -214,8 +217,8 @@ int counts_chunk(centre_ctx *ctx, const EntParams &E, int scheme, uint32_t ndof,
   P.nb = nb;
   P.nsteps = E.nsteps;
   P.all_pairs = 0;
-  CENTRE_TRY(launch_pairs_atomic(ctx, P, d_tasks, tasks.size(), (const double *)ctx_clnc(ctx),
-                                 nullptr, nullptr, d_counts));
+  CENTRE_TRY(launch_pairs_atomic(ctx, P, d_tasks, tasks.size(), nullptr, nullptr, nullptr,
+                                 d_counts));
   // the task buffer is reused by the next chunk: finish this one first
   CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return CENTRE_OK;
@@ -233,8 +236,6 @@ std::vector<uint32_t> all_pairs_list(uint32_t ndof) {
 }
 
 }  // namespace
-
-void *ctx_clnc(centre_ctx *ctx) { return ctx->d_clnc; }
 
 // ---------------------------------------------------------------------------
 int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof,
@@ -261,10 +262,12 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
     if (!d_tmp) return st;
     double *d_lsum = d_tmp + (uint64_t)ndof * per;
     CENTRE_TRY(launch_entropy1d(ctx, E, ndof, d_types, d_bins, d_ext, d_tmp, nullptr, d_lsum));
-    U128 *d_sclnc = (U128 *)scratch(ctx, kSlotMoments,
-                                    (sizeof(U128) + sizeof(unsigned)) * npairs * E.nsteps, &st);
+    const unsigned long long *d_fix = fix_table(ctx, E.fix_scale, &st);
+    if (!d_fix) return st;
+    unsigned long long *d_sclnc = (unsigned long long *)scratch(
+        ctx, kSlotMoments, (sizeof(unsigned long long) + sizeof(unsigned)) * npairs * E.nsteps,
+        &st);
     if (!d_sclnc) return st;
-    const double *d_tab = (const double *)ctx->d_clnc;
     unsigned *d_nnz = reinterpret_cast<unsigned *>(d_sclnc + npairs * E.nsteps);
     std::vector<uint32_t> h_pairs;
     for (int s = 0; s < E.nschemes; ++s) {
@@ -279,6 +282,7 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
       P.scheme = s;
       P.nb = nb;
       P.nsteps = E.nsteps;
+      P.fix_scale = E.fix_scale;
       const int form = p->counts_form;
       // AUTO takes the tensor-core contraction only where the histograms
       // do not fit shared memory (more than 217 bins; kTcAutoMaxBins is 0).
@@ -296,11 +300,11 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
                          "tensor-core counts need the all-pairs form and a supported bin count");
       if (use_tc) {
         P.all_pairs = 1;
-        CENTRE_TRY(launch_pairs_tc(ctx, P, d_tab, d_sclnc, d_nnz));
+        CENTRE_TRY(launch_pairs_tc(ctx, P, d_fix, d_sclnc, d_nnz));
       } else if (!atomic_fits(nb)) {
         // histograms too large for shared memory: one global histogram per CTA
         P.all_pairs = all ? 1 : 0;
-        CENTRE_TRY(launch_pairs_global(ctx, P, d_pairs, 0, npairs, d_tab, d_sclnc, d_nnz,
+        CENTRE_TRY(launch_pairs_global(ctx, P, d_pairs, 0, npairs, d_fix, d_sclnc, d_nnz,
                                        nullptr));
       } else {
         if (all) {
@@ -311,7 +315,7 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
           P.tile = tile;
           P.ntile = (ndof + tile - 1) / tile;
           const uint64_t ntasks = P.ntile * (P.ntile + 1) / 2;
-          CENTRE_TRY(launch_pairs_atomic(ctx, P, nullptr, ntasks, d_tab, d_sclnc, d_nnz,
+          CENTRE_TRY(launch_pairs_atomic(ctx, P, nullptr, ntasks, d_fix, d_sclnc, d_nnz,
                                          nullptr));
         } else {
           if (h_pairs.empty()) {
@@ -329,7 +333,7 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
           if (!d_tasks) return st;
           CENTRE_CUDA(ctx, cudaMemcpyAsync(d_tasks, tasks.data(), sizeof(PairTask) * tasks.size(),
                                            cudaMemcpyHostToDevice, ctx->stream));
-          CENTRE_TRY(launch_pairs_atomic(ctx, P, d_tasks, tasks.size(), d_tab, d_sclnc,
+          CENTRE_TRY(launch_pairs_atomic(ctx, P, d_tasks, tasks.size(), d_fix, d_sclnc,
                                          d_nnz, nullptr));
           CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         }
@@ -418,19 +422,11 @@ int centre_gpu_create(centre_ctx **out, int device) {
   if ((rc = check_cuda(ctx, cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking),
                        "stream")) != CENTRE_OK ||
       (rc = check_cuda(ctx, cudaMalloc(&ctx->d_flag, sizeof(int)), "flag")) != CENTRE_OK ||
-      (rc = check_cuda(ctx, cudaMallocHost(&ctx->h_flag, sizeof(int)), "flag")) != CENTRE_OK ||
-      (rc = check_cuda(ctx, cudaMalloc(&ctx->d_clnc, sizeof(double) * kTabGlobal),
-                       "table")) != CENTRE_OK) {
+      (rc = check_cuda(ctx, cudaMallocHost(&ctx->h_flag, sizeof(int)), "flag")) != CENTRE_OK) {
     centre_gpu_destroy(ctx);
     return rc;
   }
   ctx->own_stream = true;
-  rc = init_clnc_table(ctx, (double *)ctx->d_clnc);
-  if (rc == CENTRE_OK) rc = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "init");
-  if (rc != CENTRE_OK) {
-    centre_gpu_destroy(ctx);
-    return rc;
-  }
   *out = ctx;
   return CENTRE_OK;
 }
@@ -443,7 +439,8 @@ void centre_gpu_destroy(centre_ctx *ctx) {
     if (b.ptr) cudaFree(b.ptr);
   if (ctx->d_flag) cudaFree(ctx->d_flag);
   if (ctx->h_flag) cudaFreeHost(ctx->h_flag);
-  if (ctx->d_clnc) cudaFree(ctx->d_clnc);
+  for (void *t : ctx->d_fix)
+    if (t) cudaFree(t);
   for (auto &t : ctx->timers) {
     cudaEventDestroy(t.a);
     cudaEventDestroy(t.b);
@@ -668,19 +665,25 @@ int centre_gpu_counts2d(centre_ctx *ctx, const centre_entropy_params *p, uint32_
 }
 
 int centre_gpu_pair_moments(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof,
-                            const uint8_t *bins, int scheme, uint64_t *clnc, uint32_t *nnz) {
-  if (!ctx || !p || !bins || !clnc || !nnz) return set_error(ctx, CENTRE_E_ARG, "null argument");
+                            const uint8_t *bins, int scheme, uint64_t *clnc, uint32_t *nnz,
+                            int *scale) {
+  if (!ctx || !p || !bins || !clnc || !nnz || !scale)
+    return set_error(ctx, CENTRE_E_ARG, "null argument");
   cudaSetDevice(ctx->device);
   EntParams E;
   CENTRE_TRY(validate_params(ctx, p, &E));
   if (scheme < 0 || scheme >= E.nschemes) return set_error(ctx, CENTRE_E_ARG, "bad scheme");
+  *scale = E.fix_scale;
   if (ndof < 2) return CENTRE_OK;
   const uint64_t npairs = (uint64_t)ndof * (ndof - 1) / 2;
   int st = CENTRE_OK;
+  const unsigned long long *d_fix = fix_table(ctx, E.fix_scale, &st);
+  if (!d_fix) return st;
   const size_t nbb = (size_t)ndof * E.nschemes * E.nframes;
   unsigned char *d_in = (unsigned char *)scratch(ctx, kSlotIn, nbb, &st);
   if (!d_in) return st;
-  U128 *d_m = (U128 *)scratch(ctx, kSlotMoments, (sizeof(U128) + 4) * npairs * E.nsteps, &st);
+  unsigned long long *d_m = (unsigned long long *)scratch(
+      ctx, kSlotMoments, (sizeof(unsigned long long) + 4) * npairs * E.nsteps, &st);
   if (!d_m) return st;
   unsigned *d_z = reinterpret_cast<unsigned *>(d_m + npairs * E.nsteps);
   CENTRE_CUDA(ctx, cudaMemcpyAsync(d_in, bins, nbb, cudaMemcpyHostToDevice, ctx->stream));
@@ -696,10 +699,11 @@ int centre_gpu_pair_moments(centre_ctx *ctx, const centre_entropy_params *p, uin
   P.nb = E.schemes[scheme];
   P.nsteps = E.nsteps;
   P.all_pairs = 1;
+  P.fix_scale = E.fix_scale;
   if (p->counts_form == CENTRE_COUNTS_TC) {
     if (!tc_supported(ctx, P.nb, E.nframes))
       return set_error(ctx, CENTRE_E_UNSUPPORTED, "tensor-core counts not supported here");
-    CENTRE_TRY(launch_pairs_tc(ctx, P, (const double *)ctx->d_clnc, d_m, d_z));
+    CENTRE_TRY(launch_pairs_tc(ctx, P, d_fix, d_m, d_z));
   } else {
     if (!atomic_fits(P.nb))
       return set_error(ctx, CENTRE_E_UNSUPPORTED, "bin count too large for shared-memory counts");
@@ -708,11 +712,11 @@ int centre_gpu_pair_moments(centre_ctx *ctx, const centre_entropy_params *p, uin
     while ((tile + 1) * (tile + 1) <= ppair && tile < 4) ++tile;
     P.tile = tile;
     P.ntile = (ndof + tile - 1) / tile;
-    CENTRE_TRY(launch_pairs_atomic(ctx, P, nullptr, P.ntile * (P.ntile + 1) / 2,
-                                   (const double *)ctx->d_clnc, d_m, d_z, nullptr));
+    CENTRE_TRY(launch_pairs_atomic(ctx, P, nullptr, P.ntile * (P.ntile + 1) / 2, d_fix, d_m, d_z,
+                                   nullptr));
   }
   CENTRE_TRY(read_flag(ctx));
-  CENTRE_CUDA(ctx, cudaMemcpyAsync(clnc, d_m, sizeof(U128) * npairs * E.nsteps,
+  CENTRE_CUDA(ctx, cudaMemcpyAsync(clnc, d_m, sizeof(unsigned long long) * npairs * E.nsteps,
                                    cudaMemcpyDeviceToHost, ctx->stream));
   CENTRE_CUDA(ctx, cudaMemcpyAsync(nnz, d_z, 4 * npairs * E.nsteps, cudaMemcpyDeviceToHost,
                                    ctx->stream));

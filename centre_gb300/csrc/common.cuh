@@ -17,8 +17,8 @@ constexpr int kMaxBins = 255;
 constexpr int kMaxSchemes = 16;
 constexpr int kMaxSteps = 255;
 
-// Largest frame count: counts stay below 2^27, so a per-pair sum of up to
-// 65025 cells of c ln c * 2^52 fits in 128 bits.
+// Largest frame count (counts and the 64-bit moment sums stay exact below
+// it; see clnc_fix in entropy.cuh).
 constexpr uint64_t kMaxFrames = 1ull << 27;
 
 // Grow-only device scratch owned by a context.
@@ -40,7 +40,8 @@ struct centre_ctx {
   int *d_flag = nullptr;   // device error flag (bin range, timeouts)
   int *h_flag = nullptr;   // pinned mirror
   int cc_major = 0, cc_minor = 0;
-  void *d_clnc = nullptr;  // c ln c (double) for c < 2^16
+  // fixed-point c ln c tables (2^16 entries), one per moment scale s in use
+  void *d_fix[64] = {};
   // event timing of the hot kernels (centre_gpu_enable_timing)
   bool timing = false;
   struct TimerRec {
@@ -72,7 +73,6 @@ enum ScratchSlot {
 int set_error(centre_ctx *ctx, int status, const std::string &msg);
 int check_cuda(centre_ctx *ctx, cudaError_t e, const char *what);
 void *scratch(centre_ctx *ctx, int slot, size_t bytes, int *status);
-void *ctx_clnc(centre_ctx *ctx);
 void batch_state_free(centre_ctx *ctx);
 void screen_state_free(centre_ctx *ctx);
 

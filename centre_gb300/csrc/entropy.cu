@@ -28,10 +28,10 @@
 namespace centre {
 
 // ----------------------------------------------------------------------------
-// c*ln(c) fixed-point table
-__global__ void clnc_table_kernel(double *t, int n) {
+// Fixed-point c ln c table at moment scale s (see clnc_fix)
+__global__ void fix_table_kernel(unsigned long long *t, int n, int s) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < n) t[c] = clnc_value((unsigned)c);
+  if (c < n) t[c] = clnc_fix((unsigned)c, s);
 }
 
 // ----------------------------------------------------------------------------
@@ -234,8 +234,7 @@ __device__ __forceinline__ uint64_t tri_index(uint64_t i, uint64_t j, uint64_t n
   return i * n - i * (i + 1) / 2 + (j - i - 1);
 }
 
-constexpr int kTabHist = 1024;  // 128-bit c ln c entries kept in shared memory
-constexpr int kTab64 = 512;     // c ln c * 2^52 < 2^64 for these counts: 64-bit entries
+constexpr int kTabF = 2560;     // fixed-point c ln c entries kept in shared memory
 constexpr int kRedBatch = 4;    // cells per lane per batch in the moment reduction
 #ifndef CENTRE_HIST_MIN_BLOCKS
 #define CENTRE_HIST_MIN_BLOCKS 2
@@ -259,9 +258,11 @@ __device__ __forceinline__ void red_shared_inc(uint32_t addr) {
   asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr) : "memory");
 }
 
-// c ln c beyond the shared table (rare): kept out of line.
-__device__ __noinline__ U128 clnc_far_u128(const double *__restrict__ gtab, unsigned c) {
-  return u128_from_double((c < (unsigned)kTabGlobal) ? __ldg(gtab + c) : clnc_value(c));
+// F(c) beyond the shared table: the global table, or (counts of 2^16 and
+// more) the same expression the table was filled with.
+__device__ __forceinline__ unsigned long long fix_far(const unsigned long long *__restrict__ gfix,
+                                                      unsigned c, int s) {
+  return (c < (unsigned)kTabGlobal) ? __ldg(gfix + c) : clnc_fix(c, s);
 }
 
 // One R x C tile of pairs of one trajectory.
@@ -273,7 +274,8 @@ struct HistJob {
   int nschemes;
   int scheme;
   int nb;
-  U128 *sclnc;
+  int fix_scale;
+  unsigned long long *sclnc;
   unsigned *nnz;
   unsigned *counts;
 };
@@ -319,17 +321,20 @@ __device__ void decode_all_pairs_tile(uint64_t id, uint64_t ntile, uint32_t ndof
 // the busiest bank ~3.3 times (shared-memory wavefronts bound this kernel).
 // The loaded words are rotated in registers, so the loads stay coalesced.
 // The moment reduction then sweeps the whole tile with the CTA: a lane's
-// words all belong to pair l mod NP (it needs the 64-bit table of the
-// batched reduction and 512 threads: 16 warps combine through shared memory).
+// words all belong to pair l mod NP (512 threads: 16 warps combine through
+// shared memory).
 // With kIlv the next 4-frame group's words are also loaded before the
 // current group's increments (kHistPrefetch).
+// `tabf` holds F(c) (the fixed-point c ln c of clnc_fix) for c < kTabF in
+// shared memory, `gfix` for c < 2^16 in global memory.
 template <int R, int C, bool kCounts, bool kBatchedRed, bool kIlv = false>
 __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_t *cols_s,
-                         const uint64_t *out_s, unsigned *hist, const U128 *tab,
-                         const unsigned long long *tab64, const double *__restrict__ gtab) {
+                         const uint64_t *out_s, unsigned *hist,
+                         const unsigned long long *tabf,
+                         const unsigned long long *__restrict__ gfix) {
   constexpr int NP = R * C;
   static_assert(!kIlv || (32 % NP == 0 && NP > 1), "interleaving needs NP | 32");
-  static_assert(!kIlv || kBatchedRed, "the interleaved reduction reads the 64-bit table");
+  static_assert(!kIlv || kBatchedRed, "the interleaved reduction takes cells in batches");
   constexpr bool kPrefetch = kIlv && kHistPrefetch;
   const int tid = threadIdx.x;
   const int nb = J.nb, nb2 = nb * nb;
@@ -346,6 +351,14 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
   // word path is used; the byte path rebuilds the byte offset)
   const uint32_t *bw = reinterpret_cast<const uint32_t *>(bins);
   const uint32_t nb4 = 4u * (uint32_t)nb;
+  // Bin range check four bytes at a time.  Up to 128 bins a byte x is out
+  // of range (x >= nb) exactly when bit 7 of x | (x + 128 - nb) is set: below
+  // 128, x + 128 - nb stays below 256 and reaches 128 exactly when x >= nb;
+  // from 128 on, x itself has bit 7.  A carry out of an out-of-range byte can
+  // only flag its neighbour, and the word is rejected either way.  Above 128
+  // bins the vector compare does it.
+  const bool small_nb = nb <= 128;
+  const uint32_t range_add = small_nb ? 0x01010101u * (uint32_t)(128 - nb) : 0u;
   const uint32_t lim = 0x01010101u * (uint32_t)nb;
   // 32-bit loads need every row start 4-byte aligned: the frame count and
   // the caller's bins pointer (an offset view may not be)
@@ -371,19 +384,27 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
     }
   };
   // x rotated by k places (y[i] = x[(i + k) mod N]) with selects: no
-  // dynamically indexed registers
+  // dynamically indexed registers (four entries: by 1, then by 2)
   auto rotate = [](auto &x, int k) {
     constexpr int N = sizeof(x) / sizeof(x[0]);
-    uint32_t y[N];
+    if constexpr (N == 4) {
+      uint32_t y[4];
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-      uint32_t v = x[i];
+      for (int i = 0; i < 4; ++i) y[i] = (k & 1) ? x[(i + 1) & 3] : x[i];
 #pragma unroll
-      for (int j = 1; j < N; ++j) v = (k == j) ? x[(i + j) % N] : v;
-      y[i] = v;
+      for (int i = 0; i < 4; ++i) x[i] = (k & 2) ? y[(i + 2) & 3] : y[i];
+    } else {
+      uint32_t y[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        uint32_t v = x[i];
+#pragma unroll
+        for (int j = 1; j < N; ++j) v = (k == j) ? x[(i + j) % N] : v;
+        y[i] = v;
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) x[i] = y[i];
     }
-#pragma unroll
-    for (int i = 0; i < N; ++i) x[i] = y[i];
   };
   if (!kBatchedRed) setup();
   for (int t = 0; t < J.nsteps; ++t) {
@@ -445,10 +466,18 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
           load_group(g, rw, cw);
         }
         uint32_t v = 0;
+        if (small_nb) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) v |= __vcmpgeu4(rw[r], lim);
+          for (int r = 0; r < R; ++r) v |= rw[r] | (rw[r] + range_add);
 #pragma unroll
-        for (int c = 0; c < C; ++c) v |= __vcmpgeu4(cw[c], lim);
+          for (int c = 0; c < C; ++c) v |= cw[c] | (cw[c] + range_add);
+          v &= 0x80808080u;
+        } else {
+#pragma unroll
+          for (int r = 0; r < R; ++r) v |= __vcmpgeu4(rw[r], lim);
+#pragma unroll
+          for (int c = 0; c < C; ++c) v |= __vcmpgeu4(cw[c], lim);
+        }
         if (v) {
           bad = 1;
           continue;
@@ -486,49 +515,39 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
       // the CTA sweeps all NP * nb2 words; lane l only meets pair l mod NP.
       // Sums are exact (integer), so the order does not matter.
       constexpr int kW = 16;   // warps of the 512-thread CTA
-      __shared__ U128 wacc_s[kW][NP];
+      __shared__ unsigned long long wacc_s[kW][NP];
       __shared__ unsigned wnz_s[kW][NP];
       const int warp = tid >> 5, lane = tid & 31;
       const int tot = NP * nb2, stride = (int)blockDim.x;
-      U128 acc;
-      acc.lo = acc.hi = 0ull;
+      unsigned long long acc = 0ull;
       unsigned cz = 0;
-      // warp-uniform trip count (the warp votes below need every lane)
+      // warp-uniform trip count (the warp vote below needs every lane)
       for (int k0 = warp * 32; k0 < tot; k0 += stride * kRedBatch) {
         unsigned c[kRedBatch];
-        U128 v[kRedBatch];
+        unsigned long long v[kRedBatch];
         bool big = false;
 #pragma unroll
         for (int u = 0; u < kRedBatch; ++u) {
           const int k = k0 + u * stride + lane;
           c[u] = (k < tot) ? hist[k] : 0u;
-          big |= c[u] >= (unsigned)kTab64;
-          v[u].lo = tab64[min(c[u], (unsigned)kTab64 - 1u)];
-          v[u].hi = 0ull;
+          big |= c[u] >= (unsigned)kTabF;
+          v[u] = tabf[min(c[u], (unsigned)kTabF - 1u)];
         }
         if (__any_sync(0xffffffffu, big)) {
-          double fv[kRedBatch];
 #pragma unroll
           for (int u = 0; u < kRedBatch; ++u)
-            if (c[u] >= (unsigned)kTabHist)
-              fv[u] = __ldg(gtab + min(c[u], (unsigned)kTabGlobal - 1u));
-#pragma unroll
-          for (int u = 0; u < kRedBatch; ++u)
-            if (c[u] >= (unsigned)kTab64)
-              v[u] = (c[u] < (unsigned)kTabHist)    ? tab[c[u]]
-                     : (c[u] < (unsigned)kTabGlobal) ? u128_from_double(fv[u])
-                                                      : clnc_far_u128(gtab, c[u]);
+            if (c[u] >= (unsigned)kTabF) v[u] = fix_far(gfix, c[u], J.fix_scale);
         }
 #pragma unroll
         for (int u = 0; u < kRedBatch; ++u) {
-          acc = u128_add(acc, v[u]);
+          acc += v[u];
           cz += (c[u] != 0);
         }
       }
       // lanes l, l + NP, ... hold the same pair
 #pragma unroll
       for (int off = 16; off >= NP; off >>= 1) {
-        acc = u128_add(acc, u128_shfl_xor(acc, off));
+        acc += __shfl_xor_sync(0xffffffffu, acc, off);
         cz += __shfl_xor_sync(0xffffffffu, cz, off);
       }
       if (lane < NP) {
@@ -539,74 +558,60 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
       if (tid < NP) {
         const uint64_t o = out_s[tid];
         if (o != ~0ull) {
-          U128 s = wacc_s[0][tid];
-          unsigned z = wnz_s[0][tid];
-          for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-            s = u128_add(s, wacc_s[w][tid]);
+          unsigned long long sum = 0ull;
+          unsigned z = 0;
+          for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            sum += wacc_s[w][tid];
             z += wnz_s[w][tid];
           }
-          J.sclnc[o * J.nsteps + t] = s;
+          J.sclnc[o * J.nsteps + t] = sum;
           J.nnz[o * J.nsteps + t] = z;
         }
       }
     } else {
-      // one warp per pair: exact sum of c ln c and non-empty cells
+      // one warp per pair: the moment and the non-empty cells
       const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
       for (int q = warp; q < NP; q += nwarps) {
         const uint64_t o = out_s[q];
         if (o == ~0ull) continue;
-        U128 acc;
-        acc.lo = acc.hi = 0ull;
+        unsigned long long acc = 0ull;
         unsigned cz = 0;
         const unsigned *h = hist + q * nb2;
         if (kBatchedRed) {
           for (int i0 = 0; i0 < nb2; i0 += 32 * kRedBatch) {
-            // kRedBatch cells per lane: counts below kTab64 from the 64-bit
-            // shared table (half the bytes of the 128-bit one: the data pipe
-            // bounds this kernel), the rest from the 128-bit table or, beyond
-            // it (common at few bins), from the global table, loaded together
+            // kRedBatch cells per lane, table loads issued together; counts
+            // beyond the shared table (common at few bins) from the global one
             unsigned c[kRedBatch];
-            U128 v[kRedBatch];
+            unsigned long long v[kRedBatch];
             bool big = false;
 #pragma unroll
             for (int u = 0; u < kRedBatch; ++u) {
               const int i = i0 + 32 * u + lane;
               c[u] = (i < nb2) ? h[i] : 0u;
-              big |= c[u] >= (unsigned)kTab64;
-              v[u].lo = tab64[min(c[u], (unsigned)kTab64 - 1u)];
-              v[u].hi = 0ull;
+              big |= c[u] >= (unsigned)kTabF;
+              v[u] = tabf[min(c[u], (unsigned)kTabF - 1u)];
             }
             if (__any_sync(0xffffffffu, big)) {
-              double fv[kRedBatch];
 #pragma unroll
               for (int u = 0; u < kRedBatch; ++u)
-                if (c[u] >= (unsigned)kTabHist)
-                  fv[u] = __ldg(gtab + min(c[u], (unsigned)kTabGlobal - 1u));
-#pragma unroll
-              for (int u = 0; u < kRedBatch; ++u)
-                if (c[u] >= (unsigned)kTab64)
-                  v[u] = (c[u] < (unsigned)kTabHist)    ? tab[c[u]]
-                         : (c[u] < (unsigned)kTabGlobal) ? u128_from_double(fv[u])
-                                                          : clnc_far_u128(gtab, c[u]);
+                if (c[u] >= (unsigned)kTabF) v[u] = fix_far(gfix, c[u], J.fix_scale);
             }
 #pragma unroll
             for (int u = 0; u < kRedBatch; ++u) {
-              acc = u128_add(acc, v[u]);
+              acc += v[u];
               cz += (c[u] != 0);
             }
           }
         } else {
-          // one cell at a time (fewer registers: more resident CTAs; a
-          // 64-bit table for small counts was measured slower here)
+          // one cell at a time (fewer registers: more resident CTAs)
           for (int i = lane; i < nb2; i += 32) {
             const unsigned c = h[i];
-            const U128 v = (c < (unsigned)kTabHist) ? tab[c] : clnc_far_u128(gtab, c);
-            acc = u128_add(acc, v);
+            acc += (c < (unsigned)kTabF) ? tabf[c] : fix_far(gfix, c, J.fix_scale);
             cz += (c != 0);
           }
         }
         for (int off = 16; off; off >>= 1) {
-          acc = u128_add(acc, u128_shfl_xor(acc, off));
+          acc += __shfl_xor_sync(0xffffffffu, acc, off);
           cz += __shfl_xor_sync(0xffffffffu, cz, off);
         }
         if (lane == 0) {
@@ -626,15 +631,16 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
 template <int R, int C, bool kCounts, int kMinBlocks = kHistMinBlocks>
 __global__ void __launch_bounds__(512, kMinBlocks)
 pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__ tasks,
-                  const __grid_constant__ PairParams P, const double *__restrict__ gtab,
-                  U128 *__restrict__ sclnc, unsigned *__restrict__ nnz,
+                  const __grid_constant__ PairParams P,
+                  const unsigned long long *__restrict__ gfix,
+                  unsigned long long *__restrict__ sclnc, unsigned *__restrict__ nnz,
                   unsigned *__restrict__ counts, int *__restrict__ flag) {
   constexpr int NP = R * C;
   extern __shared__ __align__(16) unsigned char dyn[];
   const int nb2 = P.nb * P.nb;
   unsigned *hist = reinterpret_cast<unsigned *>(dyn);
-  U128 *tab = reinterpret_cast<U128 *>(dyn + (((size_t)NP * nb2 * 4 + 15) & ~size_t(15)));
-  unsigned long long *tab64 = reinterpret_cast<unsigned long long *>(tab + kTabHist);
+  unsigned long long *tabf =
+      reinterpret_cast<unsigned long long *>(dyn + (((size_t)NP * nb2 * 4 + 15) & ~size_t(15)));
   __shared__ uint32_t rows_s[R], cols_s[C];
   __shared__ uint64_t out_s[NP];
   const int tid = threadIdx.x;
@@ -650,8 +656,8 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
           out_s[r * C + c] = (r < tk.nr && c < tk.nc) ? tk.out[r * tk.nc + c] : ~0ull;
     }
   }
-  for (int i = tid; i < kTabHist; i += blockDim.x) tab[i] = u128_from_double(__ldg(gtab + i));
-  for (int i = tid; i < kTab64; i += blockDim.x) tab64[i] = u128_from_double(__ldg(gtab + i)).lo;
+  if (!kCounts)   // the counts mode writes counts and reads no table
+    for (int i = tid; i < kTabF; i += blockDim.x) tabf[i] = __ldg(gfix + i);
   for (int i = tid; i < NP * nb2; i += blockDim.x) hist[i] = 0;
   __syncthreads();
   HistJob J;
@@ -662,11 +668,12 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
   J.nschemes = P.nschemes;
   J.scheme = P.scheme;
   J.nb = P.nb;
+  J.fix_scale = P.fix_scale;
   J.sclnc = sclnc;
   J.nnz = nnz;
   J.counts = counts;
   const int bad = hist_tile<R, C, kCounts, true, kHistInterleave && R == 4 && C == 4>(
-      J, rows_s, cols_s, out_s, hist, tab, tab64, gtab);
+      J, rows_s, cols_s, out_s, hist, tabf, gfix);
   if (bad && tid == 0) atomicOr(flag, kFlagBinRange);
 }
 
@@ -675,18 +682,19 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
 template <int R>
 __global__ void __launch_bounds__(512)
 pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nitems,
-                        const __grid_constant__ BatchCommon B, const double *__restrict__ gtab,
-                        int *__restrict__ flag) {
+                        const __grid_constant__ BatchCommon B,
+                        const unsigned long long *__restrict__ gfix, int *__restrict__ flag) {
   constexpr int NP = R * R;
   extern __shared__ __align__(16) unsigned char dyn[];
   const int nb2 = B.nb * B.nb;
   unsigned *hist = reinterpret_cast<unsigned *>(dyn);
-  U128 *tab = reinterpret_cast<U128 *>(dyn + (((size_t)NP * nb2 * 4 + 15) & ~size_t(15)));
+  unsigned long long *tabf =
+      reinterpret_cast<unsigned long long *>(dyn + (((size_t)NP * nb2 * 4 + 15) & ~size_t(15)));
   __shared__ uint32_t rows_s[R], cols_s[R];
   __shared__ uint64_t out_s[NP];
   __shared__ int sys_s;
   const int tid = threadIdx.x;
-  for (int i = tid; i < kTabHist; i += blockDim.x) tab[i] = u128_from_double(__ldg(gtab + i));
+  for (int i = tid; i < kTabF; i += blockDim.x) tabf[i] = __ldg(gfix + i);
   for (int i = tid; i < NP * nb2; i += blockDim.x) hist[i] = 0;
   int bad = 0;
   for (uint64_t item = blockIdx.x + B.item0; item < nitems; item += gridDim.x) {
@@ -712,10 +720,11 @@ pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nit
     J.nschemes = B.nschemes;
     J.scheme = B.scheme;
     J.nb = B.nb;
+    J.fix_scale = B.fix_scale;
     J.sclnc = S.sclnc;
     J.nnz = S.nnz;
     J.counts = nullptr;
-    bad |= hist_tile<R, R, false, false>(J, rows_s, cols_s, out_s, hist, tab, nullptr, gtab);
+    bad |= hist_tile<R, R, false, false>(J, rows_s, cols_s, out_s, hist, tabf, gfix);
   }
   if (bad) atomicOr(flag, kFlagBinRange);
 }
@@ -730,13 +739,14 @@ pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nit
 __global__ void __launch_bounds__(512)
 pairs_global_kernel(const uint8_t *__restrict__ bins, const __grid_constant__ PairParams P,
                     const uint32_t *__restrict__ pairs, uint64_t p0, uint64_t np,
-                    const double *__restrict__ gtab, U128 *__restrict__ sclnc,
-                    unsigned *__restrict__ nnz, unsigned *__restrict__ counts,
-                    unsigned *__restrict__ hist_all, int *__restrict__ flag) {
+                    const unsigned long long *__restrict__ gfix,
+                    unsigned long long *__restrict__ sclnc, unsigned *__restrict__ nnz,
+                    unsigned *__restrict__ counts, unsigned *__restrict__ hist_all,
+                    int *__restrict__ flag) {
   const int nb = P.nb, nb2 = nb * nb;
   unsigned *h = hist_all + (uint64_t)blockIdx.x * nb2;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  __shared__ U128 wacc[32];
+  __shared__ unsigned long long wacc[32];
   __shared__ unsigned wnz[32];
   int bad = 0;
   for (uint64_t q = blockIdx.x; q < np; q += gridDim.x) {
@@ -765,17 +775,15 @@ pairs_global_kernel(const uint8_t *__restrict__ bins, const __grid_constant__ Pa
         unsigned *dst = counts + (q * P.nsteps + t) * (uint64_t)nb2;
         for (int c = tid; c < nb2; c += blockDim.x) dst[c] = __ldcg(h + c);
       } else {
-        U128 acc;
-        acc.lo = acc.hi = 0ull;
+        unsigned long long acc = 0ull;
         unsigned cz = 0;
         for (int c = tid; c < nb2; c += blockDim.x) {
           const unsigned v = __ldcg(h + c);
-          acc = u128_add(acc, u128_from_double(v < (unsigned)kTabGlobal ? __ldg(gtab + v)
-                                                                      : clnc_value(v)));
+          acc += fix_far(gfix, v, P.fix_scale);
           cz += (v != 0);
         }
         for (int off = 16; off; off >>= 1) {
-          acc = u128_add(acc, u128_shfl_xor(acc, off));
+          acc += __shfl_xor_sync(0xffffffffu, acc, off);
           cz += __shfl_xor_sync(0xffffffffu, cz, off);
         }
         if (lane == 0) {
@@ -784,10 +792,10 @@ pairs_global_kernel(const uint8_t *__restrict__ bins, const __grid_constant__ Pa
         }
         __syncthreads();
         if (tid == 0) {
-          U128 tot = wacc[0];
+          unsigned long long tot = wacc[0];
           unsigned z = wnz[0];
           for (int w = 1; w < nwarps; ++w) {
-            tot = u128_add(tot, wacc[w]);
+            tot += wacc[w];
             z += wnz[w];
           }
           sclnc[gp * P.nsteps + t] = tot;
@@ -804,8 +812,8 @@ pairs_global_kernel(const uint8_t *__restrict__ bins, const __grid_constant__ Pa
 }
 
 int launch_pairs_global(centre_ctx *ctx, const PairParams &P, const uint32_t *d_pairs,
-                        uint64_t p0, uint64_t np, const double *d_tab, U128 *d_sclnc,
-                        unsigned *d_nnz, unsigned *d_counts) {
+                        uint64_t p0, uint64_t np, const unsigned long long *d_fix,
+                        unsigned long long *d_sclnc, unsigned *d_nnz, unsigned *d_counts) {
   if (np == 0) return CENTRE_OK;
   const uint64_t grid = std::min<uint64_t>(np, (uint64_t)ctx->sm_count * 4);
   int st = CENTRE_OK;
@@ -815,7 +823,7 @@ int launch_pairs_global(centre_ctx *ctx, const PairParams &P, const uint32_t *d_
   CENTRE_CUDA(ctx, cudaMemsetAsync(d_hist, 0, sizeof(unsigned) * grid * (uint64_t)P.nb * P.nb,
                                    ctx->stream));
   KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
-  pairs_global_kernel<<<(unsigned)grid, 512, 0, ctx->stream>>>(P.bins, P, d_pairs, p0, np, d_tab,
+  pairs_global_kernel<<<(unsigned)grid, 512, 0, ctx->stream>>>(P.bins, P, d_pairs, p0, np, d_fix,
                                                              d_sclnc, d_nnz, d_counts, d_hist,
                                                              ctx->d_flag);
   ctx->launches++;
@@ -829,7 +837,7 @@ int launch_pairs_global(centre_ctx *ctx, const PairParams &P, const uint32_t *d_
 __global__ void finalize2d_kernel(const uint32_t *__restrict__ pairs, int all_pairs,
                                   uint32_t ndof, const double *__restrict__ logw,
                                   const double *__restrict__ lsum,
-                                  const U128 *__restrict__ sclnc,
+                                  const unsigned long long *__restrict__ sclnc,
                                   const unsigned *__restrict__ nnz,
                                   const __grid_constant__ EntParams P, int scheme,
                                   uint64_t npairs, double *__restrict__ s2) {
@@ -845,7 +853,7 @@ __global__ void finalize2d_kernel(const uint32_t *__restrict__ pairs, int all_pa
     j = pairs[2 * p + 1];
   }
   const double nd = (t + 1.0) * (double)P.step_size;
-  const double X = u128_value(sclnc[idx]);
+  const double X = (double)sclnc[idx] * P.fix_inv;
   const double L = lsum[((uint64_t)i * P.nschemes + scheme) * P.nsteps + t] +
                    lsum[((uint64_t)j * P.nschemes + scheme) * P.nsteps + t];
   // log(n A) = log n + log w_i + log w_j (per-step and per-DOF logs hoisted)
@@ -982,11 +990,41 @@ entropy2d_counts_kernel(const uint32_t *__restrict__ pairs, const uint8_t *__res
 }
 
 // ----------------------------------------------------------------------------
-int init_clnc_table(centre_ctx *ctx, double *tab) {
-  clnc_table_kernel<<<(kTabGlobal + 255) / 256, 256, 0, ctx->stream>>>(tab, kTabGlobal);
+int moment_scale(uint64_t n) {
+  if (n < 3) return 52;
+  const double L = (double)n * std::log((double)n);   // largest possible moment
+  const int s = 63 - (int)std::ceil(std::log2(L));
+  return std::max(0, std::min(52, s));
+}
+
+int fill_fix_table(centre_ctx *ctx, unsigned long long *tab, int s) {
+  fix_table_kernel<<<(kTabGlobal + 255) / 256, 256, 0, ctx->stream>>>(tab, kTabGlobal, s);
   ctx->launches++;
   CENTRE_CUDA(ctx, cudaGetLastError());
   return CENTRE_OK;
+}
+
+const unsigned long long *fix_table(centre_ctx *ctx, int s, int *status) {
+  if (s < 0 || s > 52) {
+    *status = set_error(ctx, CENTRE_E_ARG, "moment scale out of range");
+    return nullptr;
+  }
+  if (!ctx->d_fix[s]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, sizeof(unsigned long long) * kTabGlobal);
+    if (e != cudaSuccess) {
+      *status = check_cuda(ctx, e, "cudaMalloc(c ln c table)");
+      return nullptr;
+    }
+    const int rc = fill_fix_table(ctx, static_cast<unsigned long long *>(p), s);
+    if (rc != CENTRE_OK) {
+      cudaFree(p);
+      *status = rc;
+      return nullptr;
+    }
+    ctx->d_fix[s] = p;
+  }
+  return static_cast<const unsigned long long *>(ctx->d_fix[s]);
 }
 
 int launch_entropy1d(centre_ctx *ctx, const EntParams &P, uint32_t ndof, const uint8_t *d_types,
@@ -1001,7 +1039,7 @@ int launch_entropy1d(centre_ctx *ctx, const EntParams &P, uint32_t ndof, const u
   return CENTRE_OK;
 }
 
-// Shared-memory budget of the histograms (the 128-bit c ln c table and the
+// Shared-memory budget of the histograms (the fixed-point c ln c table and the
 // kernel's static data take the rest of the 227 KB).
 #ifndef CENTRE_HIST_BUDGET_KB
 #define CENTRE_HIST_BUDGET_KB 184
@@ -1016,28 +1054,30 @@ int pair_tile_for(int nb) {
 
 template <int R, int C, int kMinB>
 static int launch_hist_mb(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
-                          uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
+                          uint64_t ntasks, const unsigned long long *d_fix,
+                          unsigned long long *d_sclnc, unsigned *d_nnz,
                           unsigned *d_counts, size_t smem) {
   if (d_counts) {
     CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, true, kMinB>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pairs_hist_kernel<R, C, true, kMinB><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
-        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+        P.bins, d_tasks, P, d_fix, d_sclnc, d_nnz, d_counts, ctx->d_flag);
   } else {
     CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, false, kMinB>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pairs_hist_kernel<R, C, false, kMinB><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
-        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+        P.bins, d_tasks, P, d_fix, d_sclnc, d_nnz, d_counts, ctx->d_flag);
   }
   return CENTRE_OK;
 }
 
 template <int R, int C>
 static int launch_hist(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
-                       uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
+                       uint64_t ntasks, const unsigned long long *d_fix,
+                          unsigned long long *d_sclnc, unsigned *d_nnz,
                        unsigned *d_counts) {
   const size_t smem =
-      (((size_t)R * C * P.nb * P.nb * 4 + 15) & ~size_t(15)) + 16 * kTabHist + 8 * kTab64;
+      (((size_t)R * C * P.nb * P.nb * 4 + 15) & ~size_t(15)) + 8 * kTabF;
   if (R == 4 && C == 4 && kHistPrefetch) {
     // the prefetching 4 x 4 kernel is built twice: capped at 64 registers
     // for two resident CTAs, and uncapped (~120 registers) for histograms
@@ -1049,21 +1089,21 @@ static int launch_hist(centre_ctx *ctx, const PairParams &P, const PairTask *d_t
     CENTRE_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                          &per_sm, pairs_hist_kernel<R, C, false, 2>, 512, smem));
     if (per_sm < 2)
-      return launch_hist_mb<R, C, 1>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts,
+      return launch_hist_mb<R, C, 1>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts,
                                      smem);
-    return launch_hist_mb<R, C, 2>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts,
+    return launch_hist_mb<R, C, 2>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts,
                                    smem);
   }
   if (d_counts) {
     CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, true>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pairs_hist_kernel<R, C, true><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
-        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+        P.bins, d_tasks, P, d_fix, d_sclnc, d_nnz, d_counts, ctx->d_flag);
   } else {
     CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, false>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pairs_hist_kernel<R, C, false><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
-        P.bins, d_tasks, P, d_tab, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+        P.bins, d_tasks, P, d_fix, d_sclnc, d_nnz, d_counts, ctx->d_flag);
   }
   return CENTRE_OK;
 }
@@ -1071,7 +1111,7 @@ static int launch_hist(centre_ctx *ctx, const PairParams &P, const PairTask *d_t
 // Sets the dynamic shared-memory limit of the batch kernel for tiles of
 // tile x tile pairs with up to nb bins (outside any stream capture).
 int prepare_pairs_hist_batch(centre_ctx *ctx, int tile, int nb) {
-  const size_t smem = (((size_t)tile * tile * nb * nb * 4 + 15) & ~size_t(15)) + 16 * kTabHist;
+  const size_t smem = (((size_t)tile * tile * nb * nb * 4 + 15) & ~size_t(15)) + 8 * kTabF;
   auto set = [&](auto kern) {
     return check_cuda(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)smem), "batch smem attribute");
@@ -1085,7 +1125,7 @@ int prepare_pairs_hist_batch(centre_ctx *ctx, int tile, int nb) {
 }
 
 size_t pairs_hist_batch_smem(int tile, int nb) {
-  return (((size_t)tile * tile * nb * nb * 4 + 15) & ~size_t(15)) + 16 * kTabHist;
+  return (((size_t)tile * tile * nb * nb * 4 + 15) & ~size_t(15)) + 8 * kTabF;
 }
 
 // Resident CTAs per SM of the batch kernel for a tile shape and block size.
@@ -1103,15 +1143,15 @@ int pairs_hist_batch_occupancy(centre_ctx *ctx, int tile, int threads, int nb, i
 
 int launch_pairs_hist_batch(centre_ctx *ctx, const BatchSys *d_sys, int nsys, uint64_t nitems,
                             const BatchCommon &B, int tile, int threads, int grid,
-                            const double *d_tab) {
+                            const unsigned long long *d_fix) {
   if (nitems <= B.item0 || grid <= 0) return CENTRE_OK;
   KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
   const size_t smem = pairs_hist_batch_smem(tile, B.nb);
   switch (tile) {
-    case 4: pairs_hist_batch_kernel<4><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_tab, ctx->d_flag); break;
-    case 3: pairs_hist_batch_kernel<3><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_tab, ctx->d_flag); break;
-    case 2: pairs_hist_batch_kernel<2><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_tab, ctx->d_flag); break;
-    default: pairs_hist_batch_kernel<1><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_tab, ctx->d_flag); break;
+    case 4: pairs_hist_batch_kernel<4><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_fix, ctx->d_flag); break;
+    case 3: pairs_hist_batch_kernel<3><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_fix, ctx->d_flag); break;
+    case 2: pairs_hist_batch_kernel<2><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_fix, ctx->d_flag); break;
+    default: pairs_hist_batch_kernel<1><<<grid, threads, smem, ctx->stream>>>(d_sys, nsys, nitems, B, d_fix, ctx->d_flag); break;
   }
   ctx->launches++;
   CENTRE_CUDA(ctx, cudaGetLastError());
@@ -1119,7 +1159,8 @@ int launch_pairs_hist_batch(centre_ctx *ctx, const BatchSys *d_sys, int nsys, ui
 }
 
 int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
-                        uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
+                        uint64_t ntasks, const unsigned long long *d_fix,
+                          unsigned long long *d_sclnc, unsigned *d_nnz,
                         unsigned *d_counts) {
   if (ntasks == 0) return CENTRE_OK;
   if ((uint64_t)P.ndof * P.nschemes * P.nframes >= kMaxHistBinBytes)
@@ -1128,18 +1169,18 @@ int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_
   int rc;
   if (P.all_pairs) {
     switch (P.tile) {
-      case 4: rc = launch_hist<4, 4>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts); break;
-      case 3: rc = launch_hist<3, 3>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts); break;
-      case 2: rc = launch_hist<2, 2>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts); break;
-      default: rc = launch_hist<1, 1>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts); break;
+      case 4: rc = launch_hist<4, 4>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
+      case 3: rc = launch_hist<3, 3>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
+      case 2: rc = launch_hist<2, 2>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
+      default: rc = launch_hist<1, 1>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
     }
   } else {
     const int w = pair_tile_for(P.nb);
-    if (w >= 16) rc = launch_hist<1, 16>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts);
-    else if (w >= 8) rc = launch_hist<1, 8>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts);
-    else if (w >= 4) rc = launch_hist<1, 4>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts);
-    else if (w >= 2) rc = launch_hist<1, 2>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts);
-    else rc = launch_hist<1, 1>(ctx, P, d_tasks, ntasks, d_tab, d_sclnc, d_nnz, d_counts);
+    if (w >= 16) rc = launch_hist<1, 16>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
+    else if (w >= 8) rc = launch_hist<1, 8>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
+    else if (w >= 4) rc = launch_hist<1, 4>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
+    else if (w >= 2) rc = launch_hist<1, 2>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
+    else rc = launch_hist<1, 1>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
   }
   ctx->launches++;
   if (rc != CENTRE_OK) return rc;
@@ -1149,7 +1190,7 @@ int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_
 
 int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uint32_t *d_pairs,
                       int all_pairs, uint32_t ndof, const double *d_ext, const double *d_lsum,
-                      const U128 *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
+                      const unsigned long long *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
                       double *d_s2) {
   const uint64_t total = npairs * P.nsteps;
   if (total == 0) return CENTRE_OK;
@@ -1169,7 +1210,7 @@ int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uin
 // As launch_finalize2d, with the log table supplied by the caller instead of
 // context scratch (used by the entry point that allocates nothing).
 int launch_finalize2d_into(centre_ctx *ctx, const EntParams &P, int scheme, uint32_t ndof,
-                           const double *d_ext, const double *d_lsum, const U128 *d_sclnc,
+                           const double *d_ext, const double *d_lsum, const unsigned long long *d_sclnc,
                            const unsigned *d_nnz, uint64_t npairs, double *d_logw,
                            double *d_s2) {
   const uint64_t total = npairs * P.nsteps;

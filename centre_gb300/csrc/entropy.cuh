@@ -21,6 +21,8 @@ struct EntParams {
   uint8_t schemes[kMaxSchemes];
   int scheme_off[kMaxSchemes];
   uint8_t ests[4];
+  int fix_scale;        // moment scale s of the joint counts (moment_scale())
+  double fix_inv;       // 2^-s
 };
 
 // A tile of pairs handled by one CTA of the atomic count kernel.
@@ -31,11 +33,6 @@ struct PairTask {
   uint8_t nr, nc;
 };
 
-// Unsigned 128-bit accumulator for the per-cell c ln c terms.
-struct __align__(16) U128 {
-  unsigned long long lo, hi;
-};
-
 // One trajectory of a batch (device copy; see batch.cu).
 struct BatchSys {
   const uint8_t *bins;
@@ -44,7 +41,7 @@ struct BatchSys {
   uint64_t ntile;        // tiles per side of the all-pairs grid
   uint64_t item_begin;   // first work item of this trajectory
   uint32_t ndof;
-  U128 *sclnc;
+  unsigned long long *sclnc;
   unsigned *nnz;
 };
 
@@ -54,6 +51,7 @@ struct BatchCommon {
   int nschemes;
   int scheme;
   int nb;
+  int fix_scale;         // moment scale s (counts beyond the table)
 };
 
 struct PairParams {
@@ -68,24 +66,10 @@ struct PairParams {
   int nsteps;
   int all_pairs;
   int tile;             // DOFs per tile side (all-pairs mode)
+  int fix_scale;        // moment scale s (counts beyond the table)
 };
 
-constexpr int kTabSmem = 1024;      // c ln c entries kept in shared memory
-constexpr int kTabGlobal = 1 << 16; // entries in the global table
-
-__device__ __forceinline__ U128 u128_add(U128 a, U128 b) {
-  U128 r;
-  asm("add.cc.u64 %0, %2, %4;\n\taddc.u64 %1, %3, %5;"
-      : "=l"(r.lo), "=l"(r.hi)
-      : "l"(a.lo), "l"(a.hi), "l"(b.lo), "l"(b.hi));
-  return r;
-}
-
-__device__ __forceinline__ U128 u128_shfl_xor(U128 v, int o) {
-  v.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
-  v.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
-  return v;
-}
+constexpr int kTabGlobal = 1 << 16; // entries of a fixed-point c ln c table
 
 // c*log(c) in double precision, the per-cell term of the joint entropy.
 // Every count form evaluates it through this one expression (or reads it
@@ -95,34 +79,21 @@ __device__ __forceinline__ double clnc_value(unsigned c) {
   return (c < 2) ? 0.0 : (double)c * log((double)c);
 }
 
-// A non-negative double v (0 or >= 1) represented exactly as an integer
-// multiple of 2^-52: its 53-bit significand shifted by its exponent (a double
-// >= 1 is a multiple of its ulp >= 2^-52, so the shift is a left shift and
-// nothing is rounded).  Integer sums of these are the exact sums of the
-// per-cell doubles, so the cell sum is independent of how cells are spread
-// over threads, tiles or count kernels.  c ln c < 2^12 (counts below 630)
-// fits in the low word alone.
-constexpr int kFixShift = 52;   // fixed point: value * 2^52
-__device__ __forceinline__ U128 u128_from_double(double v) {
-  U128 r;
-  r.lo = 0ull;
-  r.hi = 0ull;
-  // integer test for +-0 (no FP64 instruction: FP64 issue is scarce on this part)
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-  if ((bits << 1) == 0ull) return r;
-  // value * 2^52 = m * 2^(e - 1023), e the biased exponent
-  const int s = (int)((bits >> 52) & 0x7ff) - 1023 + (kFixShift - 52);
-  const unsigned long long m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  if (s >= 64) {
-    r.hi = m << (s - 64);
-  } else {
-    r.lo = m << s;
-    r.hi = s ? (m >> (64 - s)) : 0ull;
-  }
-  return r;
+// The joint-count moments.  Per pair and step the count kernels produce
+//     X = sum over cells of F(c),   F(c) = round(c ln c * 2^s),
+// an unsigned 64-bit integer, and the number of non-empty cells.  The scale s
+// is fixed per call from the frames used, n (moment_scale): the largest s <= 52
+// with n ln n * 2^s <= 2^63, so no sum of cells (at most n ln n plus half a
+// unit per cell) can overflow.  Every count form reads F from the same table
+// (or evaluates the same expression beyond it), and integer sums do not
+// depend on their order, so all forms give the same X to the last bit.  The
+// rounding of F is at most 2^-(s+1) per cell, so X * 2^-s differs from the
+// double sum of c ln c by at most cells * 2^-(s+1): with 2^-s <= 2 n ln n /
+// 2^63 that moves an entropy (X/n) by less than cells * ln n / 2^63, about
+// 1e-13 at 255 bins and 2^27 frames.
+__device__ __forceinline__ unsigned long long clnc_fix(unsigned c, int s) {
+  return __double2ull_rn(clnc_value(c) * ldexp(1.0, s));
 }
-
-__device__ __forceinline__ U128 clnc_fixed(unsigned c) { return u128_from_double(clnc_value(c)); }
 
 // Row-major upper-triangular pair (i, j), i < j, of index p among all pairs
 // of n items: a single-precision estimate of the row, corrected exactly with
@@ -143,35 +114,38 @@ __device__ __forceinline__ void tri_pair(uint64_t p, uint64_t n, uint32_t &i, ui
   j = (uint32_t)(p - start(r) + (uint64_t)r + 1);
 }
 
-__host__ __device__ __forceinline__ double u128_value(U128 x) {
-  return (double)x.hi * 0x1p12 + (double)x.lo * 0x1p-52;
-}
-
-int init_clnc_table(centre_ctx *ctx, double *tab);
+// Moment scale for n frames used (see clnc_fix).
+int moment_scale(uint64_t n);
+// Fills tab[c] = F(c) for c < kTabGlobal at scale s (one kernel launch on
+// the context's stream; no allocation).
+int fill_fix_table(centre_ctx *ctx, unsigned long long *tab, int s);
+// The context's table for scale s, built on first use (cudaMalloc: call it
+// before any stream capture).
+const unsigned long long *fix_table(centre_ctx *ctx, int s, int *status);
 int launch_entropy1d(centre_ctx *ctx, const EntParams &P, uint32_t ndof, const uint8_t *d_types,
                      const uint8_t *d_bins, const double *d_ext, double *d_s1,
                      unsigned long long *d_freq, double *d_lsum);
 int pair_tile_for(int nb);
 int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_tasks,
-                        uint64_t ntasks, const double *d_tab, U128 *d_sclnc, unsigned *d_nnz,
-                        unsigned *d_counts);
+                        uint64_t ntasks, const unsigned long long *d_fix,
+                        unsigned long long *d_sclnc, unsigned *d_nnz, unsigned *d_counts);
 int prepare_pairs_hist_batch(centre_ctx *ctx, int tile, int nb);
 size_t pairs_hist_batch_smem(int tile, int nb);
 int pairs_hist_batch_occupancy(centre_ctx *ctx, int tile, int threads, int nb, int *per_sm);
 int launch_pairs_hist_batch(centre_ctx *ctx, const BatchSys *d_sys, int nsys, uint64_t nitems,
                             const BatchCommon &B, int tile, int threads, int grid,
-                            const double *d_tab);
+                            const unsigned long long *d_fix);
 int launch_pairs_global(centre_ctx *ctx, const PairParams &P, const uint32_t *d_pairs,
-                        uint64_t p0, uint64_t np, const double *d_tab, U128 *d_sclnc,
-                        unsigned *d_nnz, unsigned *d_counts);
+                        uint64_t p0, uint64_t np, const unsigned long long *d_fix,
+                        unsigned long long *d_sclnc, unsigned *d_nnz, unsigned *d_counts);
 int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uint32_t *d_pairs,
                       int all_pairs, uint32_t ndof, const double *d_ext, const double *d_lsum,
-                      const U128 *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
+                      const unsigned long long *d_sclnc, const unsigned *d_nnz, uint64_t npairs,
                       double *d_s2);
 int launch_finalize2d_into(centre_ctx *ctx, const EntParams &P, int scheme, uint32_t ndof,
-                           const double *d_ext, const double *d_lsum, const U128 *d_sclnc,
-                           const unsigned *d_nnz, uint64_t npairs, double *d_logw,
-                           double *d_s2);
+                           const double *d_ext, const double *d_lsum,
+                           const unsigned long long *d_sclnc, const unsigned *d_nnz,
+                           uint64_t npairs, double *d_logw, double *d_s2);
 int launch_entropy2d_counts(centre_ctx *ctx, const EntParams &P, int scheme,
                             const uint32_t *d_pairs, const uint8_t *d_types, const double *d_ext,
                             const unsigned *d_counts, uint64_t p0, uint64_t np, uint64_t npairs,
@@ -204,8 +178,8 @@ bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes);
 // at 16 bins for the 2994-DOF chain); AUTO takes the contraction only where
 // the histograms do not fit shared memory
 constexpr int kTcAutoMaxBins = 0;
-int launch_pairs_tc(centre_ctx *ctx, const PairParams &P, const double *d_tab, U128 *d_sclnc,
-                    unsigned *d_nnz);
+int launch_pairs_tc(centre_ctx *ctx, const PairParams &P, const unsigned long long *d_fix,
+                    unsigned long long *d_sclnc, unsigned *d_nnz);
 
 // score.cu
 struct ScoreParams {

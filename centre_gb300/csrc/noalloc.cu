@@ -12,10 +12,13 @@
 //
 // The array exists once per device for the life of the process and every
 // call shares it: the first call on a device records the array's address
-// (cudaGetSymbolAddress, with that device current) and fills the c*ln(c)
-// table kept at its start; later calls reuse both.  Calls that overlap on the
-// GPU (different streams, or different host threads on one device) race on
-// the array and must be serialised by the caller.
+// (cudaGetSymbolAddress, with that device current); a call fills the
+// fixed-point c*ln(c) table kept at the array's start when its moment scale
+// (which follows from the frame count) differs from the previous call's, and
+// reuses it otherwise.  Calls that overlap on the GPU (different streams, or
+// different host threads on one device) race on the array and must be
+// serialised by the caller.
+#include <cmath>
 #include <cstring>
 #include <mutex>
 
@@ -33,32 +36,37 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
 constexpr size_t kFlagBytes = 256;
-constexpr size_t kTableBytes = sizeof(double) * kTabGlobal;   // 512 KiB
+constexpr size_t kTableBytes = sizeof(unsigned long long) * kTabGlobal;   // 512 KiB
 
 std::mutex g_setup_mutex;
 unsigned char *g_base[kMaxDevices] = {};   // device address of the array
+int g_scale[kMaxDevices];                  // moment scale of the table in it (-1: none)
 
 size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
 
-// Once per device, with that device current: the array's device address and
-// the c ln c table at its start.  Returns 0 or a CENTRE_E_* status.
-int setup_device(int dev, cudaStream_t stream, unsigned char **base) {
+// With the device current: the array's device address (recorded on the
+// first call on the device) and the c ln c table at its start for moment
+// scale s (filled, on the call's stream, when the previous call on the device
+// used another scale).  Returns 0 or a CENTRE_E_* status.
+int setup_device(int dev, cudaStream_t stream, int s, unsigned char **base) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (g_base[dev]) {
-    *base = g_base[dev];
-    return CENTRE_OK;
+  if (!g_base[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || p == nullptr)
+      return CENTRE_E_CUDA;
+    g_base[dev] = static_cast<unsigned char *>(p);
+    g_scale[dev] = -1;
   }
-  void *p = nullptr;
-  if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || p == nullptr)
-    return CENTRE_E_CUDA;
-  unsigned char *b = static_cast<unsigned char *>(p);
-  centre_ctx c;
-  c.device = dev;
-  c.stream = stream;
-  if (init_clnc_table(&c, reinterpret_cast<double *>(b + kFlagBytes)) != CENTRE_OK)
-    return CENTRE_E_CUDA;
-  if (cudaStreamSynchronize(stream) != cudaSuccess) return CENTRE_E_CUDA;
-  g_base[dev] = b;
+  unsigned char *b = g_base[dev];
+  if (g_scale[dev] != s) {
+    centre_ctx c;
+    c.device = dev;
+    c.stream = stream;
+    if (fill_fix_table(&c, reinterpret_cast<unsigned long long *>(b + kFlagBytes), s) !=
+        CENTRE_OK)
+      return CENTRE_E_CUDA;
+    g_scale[dev] = s;
+  }
   *base = b;
   return CENTRE_OK;
 }
@@ -99,6 +107,8 @@ extern "C" int centre_gpu_entropy2d_static(const centre_entropy_params *p, uint3
     if (p->estimators[e] > CENTRE_MM) return CENTRE_E_UNSUPPORTED;
     E.ests[e] = p->estimators[e];
   }
+  E.fix_scale = moment_scale(E.step_size * E.nsteps);
+  E.fix_inv = ldexp(1.0, -E.fix_scale);
   if (ndof < 2) return CENTRE_OK;
 
   // sizes against the fixed array: reject what does not fit
@@ -107,7 +117,7 @@ extern "C" int centre_gpu_entropy2d_static(const centre_entropy_params *p, uint3
   const size_t b_s1 = align256(sizeof(double) * ndof * per1);
   const size_t b_l = align256(sizeof(double) * ndof * E.nschemes * E.nsteps);
   const size_t b_logw = align256(sizeof(double) * ((uint64_t)ndof * E.nschemes + E.nsteps));
-  const size_t b_mom = align256(sizeof(U128) * npairs * E.nsteps);
+  const size_t b_mom = align256(sizeof(unsigned long long) * npairs * E.nsteps);
   const size_t b_nnz = align256(sizeof(unsigned) * npairs * E.nsteps);
   const size_t need = kFlagBytes + kTableBytes + b_s1 + b_l + b_logw + b_mom + b_nnz;
   if (need > kStaticScratchBytes) return CENTRE_E_ARG;
@@ -116,11 +126,11 @@ extern "C" int centre_gpu_entropy2d_static(const centre_entropy_params *p, uint3
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return CENTRE_E_NODEVICE;
   cudaStream_t st = (cudaStream_t)stream;
   unsigned char *base = nullptr;
-  int rc = setup_device(dev, st, &base);
+  int rc = setup_device(dev, st, E.fix_scale, &base);
   if (rc != CENTRE_OK) return rc;
 
   int *d_flag = reinterpret_cast<int *>(base);
-  const double *d_tab = reinterpret_cast<const double *>(base + kFlagBytes);
+  const unsigned long long *d_fix = reinterpret_cast<const unsigned long long *>(base + kFlagBytes);
   size_t o = kFlagBytes + kTableBytes;
   double *d_s1 = reinterpret_cast<double *>(base + o);
   o += b_s1;
@@ -128,7 +138,7 @@ extern "C" int centre_gpu_entropy2d_static(const centre_entropy_params *p, uint3
   o += b_l;
   double *d_logw = reinterpret_cast<double *>(base + o);
   o += b_logw;
-  U128 *d_mom = reinterpret_cast<U128 *>(base + o);
+  unsigned long long *d_mom = reinterpret_cast<unsigned long long *>(base + o);
   o += b_mom;
   unsigned *d_nnz = reinterpret_cast<unsigned *>(base + o);
 
@@ -161,7 +171,8 @@ extern "C" int centre_gpu_entropy2d_static(const centre_entropy_params *p, uint3
     P.all_pairs = 1;
     P.tile = tile;
     P.ntile = (ndof + tile - 1) / tile;
-    if ((rc = launch_pairs_atomic(&c, P, nullptr, P.ntile * (P.ntile + 1) / 2, d_tab, d_mom, d_nnz,
+    P.fix_scale = E.fix_scale;
+    if ((rc = launch_pairs_atomic(&c, P, nullptr, P.ntile * (P.ntile + 1) / 2, d_fix, d_mom, d_nnz,
                                   nullptr)) != CENTRE_OK)
       return rc;
     if ((rc = launch_finalize2d_into(&c, E, s, ndof, extremes, d_lsum, d_mom, d_nnz, npairs, d_logw,

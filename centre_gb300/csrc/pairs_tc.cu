@@ -27,7 +27,8 @@
 // cumulative counts in columns [0, 256) and release the accumulator at once,
 // so the next step's MMAs overlap the rest of the epilogue: reading the
 // cumulative counts (tcgen05.ld), reducing each (row DOF, column DOF) block to
-// sum c ln c (exact 128-bit fixed point) and the non-empty cell count, and
+// sum F(c) (the 64-bit fixed-point c ln c of entropy.cuh) and the non-empty
+// cell count, and
 // adding them into the pair's moments with integer atomics (tiles split pair
 // blocks; integer addition keeps the result independent of the split).
 //
@@ -61,7 +62,7 @@ constexpr int kMinBins = 16;                // DOF slots per tile bounded below
 constexpr int kMaxSlotsA = kTileM / kMinBins + 1;  // 9
 constexpr int kMaxSlotsB = kTileN / kMinBins + 1;  // 17
 constexpr int kMaxSlots = kMaxSlotsA + kMaxSlotsB;
-constexpr int kTabTc = 1024;                // 128-bit c ln c entries in shared memory
+constexpr int kTabTc = 2048;                // fixed-point c ln c entries in shared memory
 #ifndef CENTRE_TC_PRODUCERS_PER_STAGE
 #define CENTRE_TC_PRODUCERS_PER_STAGE 3
 #endif
@@ -101,6 +102,7 @@ struct TcParams {
   int scheme;
   int nb;
   int nsteps;
+  int fix_scale;          // moment scale s (counts beyond the table)
 };
 
 // Geometry of one 128 x 256 tile of O^T O.
@@ -138,12 +140,11 @@ struct Smem {
   uint32_t sink;    // target of one-hot stores that fall outside a tile
   // per producer warp, its DOF slots of the current tile (see SlotInfo)
   SlotInfo slots[kProducerWarps][kSlotsPerWarp];
-  __align__(16) U128 tab[kTabTc];   // c ln c as 128-bit fixed point
-  // per (row DOF slot, column DOF slot) block of the tile: sum of c ln c as
-  // high part (bits 48+) and low 48 bits, both plain 64-bit sums, and the
-  // non-empty cell count; filled with shared-memory reductions
-  unsigned long long blk_lo[kMaxSlotsA * kMaxSlotsB];
-  unsigned long long blk_hi[kMaxSlotsA * kMaxSlotsB];
+  __align__(16) unsigned long long tab[kTabTc];   // F(c), fixed-point c ln c
+  // per (row DOF slot, column DOF slot) block of the tile: the sum of F over
+  // its cells and the non-empty cell count, filled with shared-memory
+  // reductions
+  unsigned long long blk_x[kMaxSlotsA * kMaxSlotsB];
   unsigned blk_nz[kMaxSlotsA * kMaxSlotsB];
 };
 
@@ -360,9 +361,9 @@ __device__ __forceinline__ void slot_info(const TcParams &P, const StageMeta &m,
   base = dof * P.nb - (isA ? m.rb : m.cb);
 }
 
-// c ln c for counts beyond the global table (rare), as 128-bit fixed point.
-// Kept out of line so the unrolled epilogue loop stays small.
-__device__ __noinline__ U128 clnc_far(unsigned c) { return clnc_fixed(c); }
+// F(c) for counts beyond the global table (rare).  Kept out of line so the
+// unrolled epilogue loop stays small.
+__device__ __noinline__ unsigned long long clnc_far(unsigned c, int s) { return clnc_fix(c, s); }
 
 // Load the lane's 4 frames (4*lane .. +3 of the chunk) of the warp's DOF
 // slots into registers.  The values are first used one chunk later
@@ -453,8 +454,9 @@ __device__ __forceinline__ void mark_clear(const uint32_t (&addr)[kLaneMarks]) {
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ gtab,
-                U128 *__restrict__ sclnc, unsigned *__restrict__ nnz, int *__restrict__ flag) {
+pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__restrict__ gfix,
+                unsigned long long *__restrict__ sclnc, unsigned *__restrict__ nnz,
+                int *__restrict__ flag) {
   extern __shared__ __align__(1024) unsigned char dyn[];
   // stages first (1024-aligned), then the bookkeeping block
   const uint32_t pad = (1024u - (smem_u32(dyn) & 1023u)) & 1023u;
@@ -468,10 +470,9 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
     uint4 z = make_uint4(0, 0, 0, 0);
     uint4 *p = reinterpret_cast<uint4 *>(stages);
     for (int i = tid; i < kStages * kStageBytes / 16; i += kThreads) p[i] = z;
-    for (int i = tid; i < kTabTc; i += kThreads) S.tab[i] = u128_from_double(gtab[i]);
+    for (int i = tid; i < kTabTc; i += kThreads) S.tab[i] = gfix[i];
     for (int i = tid; i < kMaxSlotsA * kMaxSlotsB; i += kThreads) {
-      S.blk_lo[i] = 0ull;
-      S.blk_hi[i] = 0ull;
+      S.blk_x[i] = 0ull;
       S.blk_nz[i] = 0u;
     }
   }
@@ -712,35 +713,30 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
         // serialise).  The blocks are then added to their pairs' moments,
         // one thread per block.
         const int rs = rowvalid ? rd - m.d0a : -1;     // row DOF slot
-        U128 acc;
-        acc.lo = acc.hi = 0ull;
+        unsigned long long acc = 0ull;
         unsigned cnz = 0;
         const int dcol = (m.cb + col0) / nb;           // DOF of the first column
         int cs = dcol - m.d0b;                         // column DOF slot
         int nextb = (dcol + 1) * nb - m.cb;            // first column of the next DOF
         auto flush = [&]() {
-          unsigned long long lo = acc.lo & 0xFFFFFFFFFFFFull;
-          unsigned long long hi = (acc.lo >> 48) | (acc.hi << 16);
+          unsigned long long x = acc;
           unsigned z = cnz;
 #pragma unroll
           for (int off = 1; off < 32; off <<= 1) {
             if (off >= seg_max) break;
-            const unsigned long long lo2 = __shfl_down_sync(0xffffffffu, lo, off);
-            const unsigned long long hi2 = __shfl_down_sync(0xffffffffu, hi, off);
+            const unsigned long long x2 = __shfl_down_sync(0xffffffffu, x, off);
             const unsigned z2 = __shfl_down_sync(0xffffffffu, z, off);
             if (lane + off < seg_end) {
-              lo += lo2;
-              hi += hi2;
+              x += x2;
               z += z2;
             }
           }
           if (seg_head && z) {
             const uint32_t bi = (uint32_t)(rs * kMaxSlotsB + cs);
-            red_shared_u64(smem_u32(&S.blk_lo[bi]), lo);
-            red_shared_u64(smem_u32(&S.blk_hi[bi]), hi);
+            red_shared_u64(smem_u32(&S.blk_x[bi]), x);
             red_shared_u32(smem_u32(&S.blk_nz[bi]), z);
           }
-          acc.lo = acc.hi = 0ull;
+          acc = 0ull;
           cnz = 0;
         };
 #pragma unroll 1
@@ -748,10 +744,10 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
           uint32_t v[kEpiW];
           tmem_ld_w(trow + (uint32_t)(chunk * kEpiW), v);
           tmem_wait_ld_w(v);
-          // exact integer counts from the FP32 accumulator; c ln c from the
-          // shared 128-bit table, larger counts from the global table
+          // exact integer counts from the FP32 accumulator; F(c) from the
+          // shared table, larger counts from the global table
           unsigned cnt[kEpiW];
-          U128 cv[kEpiW];
+          unsigned long long cv[kEpiW];
           bool big = false;
 #pragma unroll
           for (int q = 0; q < kEpiW; ++q) {
@@ -760,17 +756,12 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
             cv[q] = S.tab[min(cnt[q], (unsigned)kTabTc - 1u)];
           }
           if (__any_sync(0xffffffffu, big)) {
-            // counts beyond the shared table: all loads first, then convert
-            double far[kEpiW];
+            // counts beyond the shared table
 #pragma unroll
             for (int q = 0; q < kEpiW; ++q)
               if (cnt[q] >= (unsigned)kTabTc)
-                far[q] = __ldg(gtab + min(cnt[q], (unsigned)kTabGlobal - 1u));
-#pragma unroll
-            for (int q = 0; q < kEpiW; ++q)
-              if (cnt[q] >= (unsigned)kTabTc)
-                cv[q] = (cnt[q] < (unsigned)kTabGlobal) ? u128_from_double(far[q])
-                                                        : clnc_far(cnt[q]);
+                cv[q] = (cnt[q] < (unsigned)kTabGlobal) ? __ldg(gfix + cnt[q])
+                                                        : clnc_far(cnt[q], P.fix_scale);
           }
           // at most one column DOF boundary per kEpiW columns (nb >= 16):
           // cells before it close the current segment, the rest open the next
@@ -778,21 +769,20 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
           if (qb >= kEpiW) {
 #pragma unroll
             for (int q = 0; q < kEpiW; ++q) {
-              acc = u128_add(acc, cv[q]);
+              acc += cv[q];
               cnz += (cnt[q] != 0u);
             }
             continue;
           }
-          U128 a1;
-          a1.lo = a1.hi = 0ull;
+          unsigned long long a1 = 0ull;
           unsigned z1 = 0;
 #pragma unroll
           for (int q = 0; q < kEpiW; ++q) {
             if (q < qb) {
-              acc = u128_add(acc, cv[q]);
+              acc += cv[q];
               cnz += (cnt[q] != 0u);
             } else {
-              a1 = u128_add(a1, cv[q]);
+              a1 += cv[q];
               z1 += (cnt[q] != 0u);
             }
           }
@@ -809,21 +799,13 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const double *__restrict__ g
           if (z) {
             const int rdb = m.d0a + i / kMaxSlotsB, cdb = m.d0b + i % kMaxSlotsB;
             if (rdb < cdb && cdb < (int)P.ndof) {
-              const unsigned long long lo = S.blk_lo[i], hi = S.blk_hi[i];
-              U128 tot;
-              tot.lo = lo + (hi << 48);
-              tot.hi = (hi >> 16) + ((tot.lo < lo) ? 1ull : 0ull);
               const uint64_t pidx = (uint64_t)rdb * P.ndof - (uint64_t)rdb * (rdb + 1) / 2 +
                                     (uint64_t)(cdb - rdb - 1);
-              U128 *dst = sclnc + pidx * P.nsteps + t;
-              const unsigned long long old = atomicAdd(&dst->lo, tot.lo);
-              const unsigned long long carry = (old + tot.lo < old) ? 1ull : 0ull;
-              atomicAdd(&dst->hi, tot.hi + carry);
+              atomicAdd(&sclnc[pidx * P.nsteps + t], S.blk_x[i]);
               atomicAdd(&nnz[pidx * P.nsteps + t], z);
             }
           }
-          S.blk_lo[i] = 0ull;
-          S.blk_hi[i] = 0ull;
+          S.blk_x[i] = 0ull;
           S.blk_nz[i] = 0u;
         }
         ++nsnap;
@@ -853,8 +835,8 @@ bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes) {
   return true;
 }
 
-int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const double *d_tab, U128 *d_sclnc,
-                    unsigned *d_nnz) {
+int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const unsigned long long *d_fix,
+                    unsigned long long *d_sclnc, unsigned *d_nnz) {
   const int nb = PP.nb;
   const uint32_t ndof = PP.ndof;
   const uint64_t nrows = (uint64_t)ndof * nb;
@@ -878,7 +860,8 @@ int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const double *d_tab, 
   CENTRE_CUDA(ctx, cudaMemcpyAsync(d_tiles, tiles.data(), sizeof(uint2) * tiles.size(),
                                    cudaMemcpyHostToDevice, ctx->stream));
   const uint64_t npairs = (uint64_t)ndof * (ndof - 1) / 2;
-  CENTRE_CUDA(ctx, cudaMemsetAsync(d_sclnc, 0, sizeof(U128) * npairs * PP.nsteps, ctx->stream));
+  CENTRE_CUDA(ctx, cudaMemsetAsync(d_sclnc, 0, sizeof(unsigned long long) * npairs * PP.nsteps,
+                                   ctx->stream));
   CENTRE_CUDA(ctx, cudaMemsetAsync(d_nnz, 0, sizeof(unsigned) * npairs * PP.nsteps, ctx->stream));
   TcParams P;
   P.bins = PP.bins;
@@ -892,13 +875,14 @@ int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const double *d_tab, 
   P.scheme = PP.scheme;
   P.nb = nb;
   P.nsteps = PP.nsteps;
+  P.fix_scale = PP.fix_scale;
   const size_t smem = tc_smem_bytes();
   CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
   const unsigned grid = (unsigned)std::min<uint64_t>(tiles.size(), (uint64_t)ctx->sm_count);
   {
     KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
-    pairs_tc_kernel<<<grid, kThreads, smem, ctx->stream>>>(P, d_tab, d_sclnc, d_nnz, ctx->d_flag);
+    pairs_tc_kernel<<<grid, kThreads, smem, ctx->stream>>>(P, d_fix, d_sclnc, d_nnz, ctx->d_flag);
   }
   ctx->launches++;
   CENTRE_CUDA(ctx, cudaGetLastError());

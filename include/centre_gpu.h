@@ -201,11 +201,12 @@ int centre_gpu_entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p,
  *     has finished the call (it reads back an error flag).
  *   - ML and Miller-Madow estimators, shared-memory histogram counts only
  *     (CENTRE_E_UNSUPPORTED otherwise).
- *   - Sizes whose scratch exceeds the array (about 780,000 pair-steps, e.g.
- *     400 DOFs with 10 steps) are rejected with CENTRE_E_ARG before anything
+ *   - Sizes whose scratch exceeds the array (about 1.3 million pair-steps,
+ *     e.g. 500 DOFs with 10 steps) are rejected with CENTRE_E_ARG before anything
  *     runs; larger problems use centre_gpu_entropy2d_dev.
  *   - The first call on a device records the array's address and fills a
- *     table in it; make that first call before any stream capture.
+ *     table in it (refilled when a call's frame count needs another
+ *     fixed-point scale); make that first call before any stream capture.
  *   - Every call on a device shares the array: calls that overlap on the GPU
  *     (other streams, other host threads) race and must be serialised. */
 int centre_gpu_entropy2d_static(const centre_entropy_params *p, uint32_t ndof,
@@ -223,14 +224,15 @@ int centre_gpu_counts2d(centre_ctx *ctx, const centre_entropy_params *p,
 /* Integer moments of the joint counts of every pair i<j for one bin scheme,
  * as both count forms produce them (no reference counterpart: the
  * reference keeps the counts themselves, src/Estimators.cpp:130-205, and sums
- * p log p in entropy2D, :586-631).  Per pair and step: sum over cells of
- * c*ln(c) as an unsigned 128-bit integer in units of 2^-52 (clnc[2*k] low,
- * clnc[2*k+1] high word) and the number of non-empty cells.  Used to check
- * that the tensor-core and atomic forms count identically.
- *   clnc [npairs][nsteps][2] uint64, nnz [npairs][nsteps] uint32. */
+ * p log p in entropy2D, :586-631).  Per pair and step: the sum over cells of
+ * round(c*ln(c) * 2^s) as an unsigned 64-bit integer and the number of
+ * non-empty cells; s (returned in *scale) is the largest s <= 52 with
+ * n ln n * 2^s <= 2^63 for the n frames used, so no sum overflows.  Used to
+ * check that the tensor-core and atomic forms count identically.
+ *   clnc [npairs][nsteps] uint64, nnz [npairs][nsteps] uint32. */
 int centre_gpu_pair_moments(centre_ctx *ctx, const centre_entropy_params *p,
                             uint32_t ndof, const uint8_t *bins, int scheme,
-                            uint64_t *clnc, uint32_t *nnz);
+                            uint64_t *clnc, uint32_t *nnz, int *scale);
 
 /* ------------------------------------------------------------ scoring ---- */
 /* Number of doubles per (estimator, scheme, step) in the sums outputs: the

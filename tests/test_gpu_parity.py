@@ -395,14 +395,15 @@ def test_tc_counts_identical_to_atomic(gpu, orc, natoms, nframes, nsteps, nb):
     pa = make_params(nframes, nsteps, [nb], [0, 1], True, counts_form=1)
     pt = make_params(nframes, nsteps, [nb], [0, 1], True, counts_form=2)
     if nb * nb * 4 <= 200 * 1024:
-        ca, za = gpu.pair_moments(pa, bins)
-    ct, zt = gpu.pair_moments(pt, bins)
+        ca, za, sa = gpu.pair_moments(pa, bins)
+    ct, zt, st = gpu.pair_moments(pt, bins)
     xo, zo = oracle_moments(orc, bins[:, 0], nsteps, nb)
     assert np.array_equal(zt, zo)
-    xt = ct[..., 1].astype(np.float64) * 2.0 ** 12 + ct[..., 0].astype(np.float64) * 2.0 ** -52
-    np.testing.assert_allclose(xt, xo, rtol=1e-12)
+    # sum of c ln c in units of 2^-scale: each cell rounded by at most half a unit
+    xt = ct.astype(np.float64) * 2.0 ** -st
+    np.testing.assert_allclose(xt, xo, rtol=1e-12, atol=nb * nb * 2.0 ** -(st + 1))
     if nb * nb * 4 <= 200 * 1024:
-        assert np.array_equal(ct, ca) and np.array_equal(zt, za)
+        assert sa == st and np.array_equal(ct, ca) and np.array_equal(zt, za)
         s_at = gpu.entropy2d(pa, types, bins, ext)
         s_tc = gpu.entropy2d(pt, types, bins, ext)
         assert np.array_equal(s_at, s_tc)
@@ -420,10 +421,11 @@ def test_tc_counts_many_tiles_per_cta(gpu, orc, natoms, nframes, nsteps, nb):
     bins, ext, types = stack_blocks(tr, gpu, [nb])
     pa = make_params(nframes, nsteps, [nb], [0, 1], True, counts_form=1)
     pt = make_params(nframes, nsteps, [nb], [0, 1], True, counts_form=2)
-    ca, za = gpu.pair_moments(pa, bins)
+    ca, za, sa = gpu.pair_moments(pa, bins)
     for run in range(3):
-        ct, zt = gpu.pair_moments(pt, bins)
-        bad = np.nonzero(np.any(ct != ca, axis=(1, 2)) | np.any(zt != za, axis=1))[0]
+        ct, zt, st = gpu.pair_moments(pt, bins)
+        assert st == sa
+        bad = np.nonzero(np.any(ct != ca, axis=1) | np.any(zt != za, axis=1))[0]
         assert len(bad) == 0, f"run {run}: {len(bad)} pairs differ, first {bad[:5]}"
     ndof = len(bins)
     rng = np.random.default_rng(nb)
@@ -433,8 +435,8 @@ def test_tc_counts_many_tiles_per_cta(gpu, orc, natoms, nframes, nsteps, nb):
         f = orc.bin2d(bins[i, 0], bins[j, 0], nsteps, [nb]).reshape(nsteps, -1).astype(np.float64)
         x = np.where(f > 1, f * np.log(np.where(f > 0, f, 1)), 0).sum(axis=1)
         assert np.array_equal(zt[q], (f > 0).sum(axis=1)), (i, j)
-        xt = ct[q, :, 1].astype(np.float64) * 2.0 ** 12 + ct[q, :, 0].astype(np.float64) * 2.0 ** -52
-        np.testing.assert_allclose(xt, x, rtol=1e-12)
+        xt = ct[q].astype(np.float64) * 2.0 ** -st
+        np.testing.assert_allclose(xt, x, rtol=1e-12, atol=nb * nb * 2.0 ** -(st + 1))
     s_at = gpu.entropy2d(pa, types, bins, ext)
     s_tc = gpu.entropy2d(pt, types, bins, ext)
     assert np.array_equal(s_at, s_tc)
