@@ -283,6 +283,8 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
       P.nb = nb;
       P.nsteps = E.nsteps;
       P.fix_scale = E.fix_scale;
+      for (int e = 0; e < E.nests; ++e)
+        if (E.ests[e] == CENTRE_MM) P.want_nnz = 1;
       const int form = p->counts_form;
       // AUTO takes the tensor-core contraction only where the histograms
       // do not fit shared memory (more than 217 bins; kTcAutoMaxBins is 0).
@@ -700,6 +702,7 @@ int centre_gpu_pair_moments(centre_ctx *ctx, const centre_entropy_params *p, uin
   P.nsteps = E.nsteps;
   P.all_pairs = 1;
   P.fix_scale = E.fix_scale;
+  P.want_nnz = 1;
   if (p->counts_form == CENTRE_COUNTS_TC) {
     if (!tc_supported(ctx, P.nb, E.nframes))
       return set_error(ctx, CENTRE_E_UNSUPPORTED, "tensor-core counts not supported here");

@@ -327,7 +327,7 @@ __device__ void decode_all_pairs_tile(uint64_t id, uint64_t ntile, uint32_t ndof
 // current group's increments (kHistPrefetch).
 // `tabf` holds F(c) (the fixed-point c ln c of clnc_fix) for c < kTabF in
 // shared memory, `gfix` for c < 2^16 in global memory.
-template <int R, int C, bool kCounts, bool kBatchedRed, bool kIlv = false>
+template <int R, int C, bool kCounts, bool kBatchedRed, bool kIlv = false, bool kNnz = true>
 __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_t *cols_s,
                          const uint64_t *out_s, unsigned *hist,
                          const unsigned long long *tabf,
@@ -446,25 +446,14 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
       for (uint64_t f = max(f0, g1 << 2) + tid; f < f1; f += blockDim.x) one_frame(f);
       // kPrefetch: the next group's words are loaded before this group's
       // increments (the red.shared asm keeps later loads behind it)
-      uint32_t rn[R], cn[C];
       auto load_group = [&](uint64_t g, uint32_t (&x)[R], uint32_t (&y)[C]) {
 #pragma unroll
         for (int r = 0; r < R; ++r) x[r] = __ldg(bw + rw0[r] + (uint32_t)g);
 #pragma unroll
         for (int c = 0; c < C; ++c) y[c] = __ldg(bw + cw0[c] + (uint32_t)g);
       };
-      if (kPrefetch && g0 + tid < g1) load_group(g0 + tid, rn, cn);
-      for (uint64_t g = g0 + tid; g < g1; g += blockDim.x) {
-        uint32_t rw[R], cw[C];
-        if (kPrefetch) {
-#pragma unroll
-          for (int r = 0; r < R; ++r) rw[r] = rn[r];
-#pragma unroll
-          for (int c = 0; c < C; ++c) cw[c] = cn[c];
-          if (g + blockDim.x < g1) load_group(g + blockDim.x, rn, cn);
-        } else {
-          load_group(g, rw, cw);
-        }
+      // one 4-frame group: range check, rotation, 4 x R x C increments
+      auto count_group = [&](uint32_t (&rw)[R], uint32_t (&cw)[C]) {
         uint32_t v = 0;
         if (small_nb) {
 #pragma unroll
@@ -480,7 +469,7 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
         }
         if (v) {
           bad = 1;
-          continue;
+          return;
         }
         if (kIlv) {
           rotate(rw, rrot);
@@ -498,6 +487,29 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
 #pragma unroll
             for (int c = 0; c < C; ++c) red_shared_inc(ro[r] + co[c]);
         }
+      };
+      if (kPrefetch) {
+        // two register sets in turn: the next group's words load while the
+        // current group counts, without copies between iterations
+        uint32_t ra[R], ca[C], rb[R], cb[C];
+        const uint32_t bd = blockDim.x, ge = (uint32_t)g1;
+        uint32_t g = (uint32_t)(g0 + tid);
+        if (g < ge) load_group(g, ra, ca);
+        while (g < ge) {
+          if (g + bd < ge) load_group(g + bd, rb, cb);
+          count_group(ra, ca);
+          g += bd;
+          if (g >= ge) break;
+          if (g + bd < ge) load_group(g + bd, ra, ca);
+          count_group(rb, cb);
+          g += bd;
+        }
+      } else {
+        for (uint64_t g = g0 + tid; g < g1; g += blockDim.x) {
+          uint32_t rw[R], cw[C];
+          load_group(g, rw, cw);
+          count_group(rw, cw);
+        }
       }
     } else {
       for (uint64_t f = f0 + tid; f < f1; f += blockDim.x) one_frame(f);
@@ -512,47 +524,69 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
           dst[i] = kIlv ? hist[i * NP + q] : hist[q * nb2 + i];
       }
     } else if constexpr (kIlv) {
-      // the CTA sweeps all NP * nb2 words; lane l only meets pair l mod NP.
-      // Sums are exact (integer), so the order does not matter.
+      // The CTA sweeps all NP * nb2 words, four at a time: quad q holds cell
+      // q / 4 of pairs 4 (q mod 4) .. + 3, and a thread's quads all have the
+      // same q mod 4 (the stride is a multiple of 4), so it keeps one
+      // accumulator per pair of its group.  Sums are exact (integer), so the
+      // order does not matter.  kNnz: count the non-empty cells (Miller-Madow).
+      static_assert(NP == 16, "the quad sweep assumes 16 interleaved pairs");
       constexpr int kW = 16;   // warps of the 512-thread CTA
+      constexpr int kQ = 2;    // quads per lane per iteration
       __shared__ unsigned long long wacc_s[kW][NP];
       __shared__ unsigned wnz_s[kW][NP];
       const int warp = tid >> 5, lane = tid & 31;
-      const int tot = NP * nb2, stride = (int)blockDim.x;
-      unsigned long long acc = 0ull;
-      unsigned cz = 0;
+      const int nq = NP * nb2 / 4, stride = (int)blockDim.x;
+      const uint4 *h4 = reinterpret_cast<const uint4 *>(hist);
+      unsigned long long acc[4] = {0ull, 0ull, 0ull, 0ull};
+      unsigned cz[4] = {0u, 0u, 0u, 0u};
       // warp-uniform trip count (the warp vote below needs every lane)
-      for (int k0 = warp * 32; k0 < tot; k0 += stride * kRedBatch) {
-        unsigned c[kRedBatch];
-        unsigned long long v[kRedBatch];
+      for (int q0 = warp * 32; q0 < nq; q0 += stride * kQ) {
+        unsigned c[kQ][4];
+        unsigned long long v[kQ][4];
         bool big = false;
 #pragma unroll
-        for (int u = 0; u < kRedBatch; ++u) {
-          const int k = k0 + u * stride + lane;
-          c[u] = (k < tot) ? hist[k] : 0u;
-          big |= c[u] >= (unsigned)kTabF;
-          v[u] = tabf[min(c[u], (unsigned)kTabF - 1u)];
+        for (int u = 0; u < kQ; ++u) {
+          const int q = q0 + u * stride + lane;
+          const uint4 w = (q < nq) ? h4[q] : make_uint4(0u, 0u, 0u, 0u);
+          c[u][0] = w.x;
+          c[u][1] = w.y;
+          c[u][2] = w.z;
+          c[u][3] = w.w;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            big |= c[u][i] >= (unsigned)kTabF;
+            v[u][i] = tabf[min(c[u][i], (unsigned)kTabF - 1u)];
+          }
         }
         if (__any_sync(0xffffffffu, big)) {
 #pragma unroll
-          for (int u = 0; u < kRedBatch; ++u)
-            if (c[u] >= (unsigned)kTabF) v[u] = fix_far(gfix, c[u], J.fix_scale);
+          for (int u = 0; u < kQ; ++u)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if (c[u][i] >= (unsigned)kTabF) v[u][i] = fix_far(gfix, c[u][i], J.fix_scale);
         }
 #pragma unroll
-        for (int u = 0; u < kRedBatch; ++u) {
-          acc += v[u];
-          cz += (c[u] != 0);
-        }
-      }
-      // lanes l, l + NP, ... hold the same pair
+        for (int u = 0; u < kQ; ++u)
 #pragma unroll
-      for (int off = 16; off >= NP; off >>= 1) {
-        acc += __shfl_xor_sync(0xffffffffu, acc, off);
-        cz += __shfl_xor_sync(0xffffffffu, cz, off);
+          for (int i = 0; i < 4; ++i) {
+            acc[i] += v[u][i];
+            if (kNnz) cz[i] += (c[u][i] != 0);
+          }
       }
-      if (lane < NP) {
-        wacc_s[warp][lane] = acc;
-        wnz_s[warp][lane] = cz;
+      // lanes l, l + 4, ... hold the same four pairs
+#pragma unroll
+      for (int off = 4; off < 32; off <<= 1)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off);
+          if (kNnz) cz[i] += __shfl_xor_sync(0xffffffffu, cz[i], off);
+        }
+      if (lane < 4) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          wacc_s[warp][4 * lane + i] = acc[i];
+          wnz_s[warp][4 * lane + i] = cz[i];
+        }
       }
       __syncthreads();
       if (tid < NP) {
@@ -565,7 +599,7 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
             z += wnz_s[w][tid];
           }
           J.sclnc[o * J.nsteps + t] = sum;
-          J.nnz[o * J.nsteps + t] = z;
+          if (kNnz) J.nnz[o * J.nsteps + t] = z;
         }
       }
     } else {
@@ -628,7 +662,7 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
   return bad;
 }
 
-template <int R, int C, bool kCounts, int kMinBlocks = kHistMinBlocks>
+template <int R, int C, bool kCounts, int kMinBlocks = kHistMinBlocks, bool kNnz = true>
 __global__ void __launch_bounds__(512, kMinBlocks)
 pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__ tasks,
                   const __grid_constant__ PairParams P,
@@ -672,7 +706,7 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
   J.sclnc = sclnc;
   J.nnz = nnz;
   J.counts = counts;
-  const int bad = hist_tile<R, C, kCounts, true, kHistInterleave && R == 4 && C == 4>(
+  const int bad = hist_tile<R, C, kCounts, true, kHistInterleave && R == 4 && C == 4, kNnz>(
       J, rows_s, cols_s, out_s, hist, tabf, gfix);
   if (bad && tid == 0) atomicOr(flag, kFlagBinRange);
 }
@@ -1062,10 +1096,16 @@ static int launch_hist_mb(centre_ctx *ctx, const PairParams &P, const PairTask *
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pairs_hist_kernel<R, C, true, kMinB><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
         P.bins, d_tasks, P, d_fix, d_sclnc, d_nnz, d_counts, ctx->d_flag);
-  } else {
+  } else if (P.want_nnz) {
     CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, false, kMinB>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pairs_hist_kernel<R, C, false, kMinB><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
+        P.bins, d_tasks, P, d_fix, d_sclnc, d_nnz, d_counts, ctx->d_flag);
+  } else {
+    // no estimator needs the non-empty cell counts: they are not kept
+    CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_hist_kernel<R, C, false, kMinB, false>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pairs_hist_kernel<R, C, false, kMinB, false><<<(unsigned)ntasks, 512, smem, ctx->stream>>>(
         P.bins, d_tasks, P, d_fix, d_sclnc, d_nnz, d_counts, ctx->d_flag);
   }
   return CENTRE_OK;

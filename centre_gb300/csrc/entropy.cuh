@@ -67,6 +67,8 @@ struct PairParams {
   int all_pairs;
   int tile;             // DOFs per tile side (all-pairs mode)
   int fix_scale;        // moment scale s (counts beyond the table)
+  int want_nnz;         // non-empty cell counts needed (Miller-Madow); the
+                        // 4 x 4 histogram kernel skips them otherwise
 };
 
 constexpr int kTabGlobal = 1 << 16; // entries of a fixed-point c ln c table

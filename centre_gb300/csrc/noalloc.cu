@@ -172,6 +172,8 @@ extern "C" int centre_gpu_entropy2d_static(const centre_entropy_params *p, uint3
     P.tile = tile;
     P.ntile = (ndof + tile - 1) / tile;
     P.fix_scale = E.fix_scale;
+    for (int e = 0; e < E.nests; ++e)
+      if (E.ests[e] == CENTRE_MM) P.want_nnz = 1;
     if ((rc = launch_pairs_atomic(&c, P, nullptr, P.ntile * (P.ntile + 1) / 2, d_fix, d_mom, d_nnz,
                                   nullptr)) != CENTRE_OK)
       return rc;
