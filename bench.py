@@ -50,10 +50,15 @@ SM_COUNT = 152
 # wavefront per cycle).
 INCREMENTS_PER_SM_CYCLE = 32
 # DRAM bytes (read + written) of one pair-count launch of the default
-# workload, from an ncu capture of that launch (gpu__time_duration and the
-# two dram__bytes metrics: one pass).  None until measured for the build.
-PAIR_HIST_TRAFFIC = None
-PAIR_HIST_TRAFFIC_NOTE = None
+# workload (2994 DOFs, 100,000 frames, 50 bins, 10 steps, ML), from an ncu
+# capture of that launch: gpu__time_duration and the two dram__bytes
+# metrics, one pass (profiles/pairs_hist_chain1000_dram.md).  Algorithmic
+# bytes of the launch: the 0.30 GB bin matrix read once and 0.36 GB of
+# 64-bit moments written.
+PAIR_HIST_TRAFFIC = 1.10e9 + 0.354e9
+PAIR_HIST_TRAFFIC_NOTE = ("dram__bytes_read.sum 1.10 GB + dram__bytes_write.sum 0.354 GB of one "
+                          "ncu capture of this launch on this workload (algorithmic: 0.30 GB "
+                          "of bins read once + 0.36 GB of moments written)")
 
 
 def slowest_rank(value, dist, device="cpu"):

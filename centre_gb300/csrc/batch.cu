@@ -197,6 +197,7 @@ extern "C" int centre_gpu_entropy_batch_dev(centre_ctx *ctx, const centre_entrop
       b.step_size = E[k].step_size;
       b.ndof = sys[k].ndof;
       b.ntile = (sys[k].ndof + tile - 1) / tile;
+      b.stripe = all_pairs_stripe(tile, sys[k].nframes, b.ntile);
       b.item_begin = items;
       b.sclnc = reinterpret_cast<unsigned long long *>(base + off_m[k]);
       b.nnz = reinterpret_cast<unsigned *>(base + off_z[k]);

@@ -281,18 +281,37 @@ struct HistJob {
 };
 
 // Fill rows/cols/outputs of the all-pairs tile `id` of an upper-triangular
-// grid of R x R tiles over ndof DOFs (thread 0).
+// grid of R x R tiles over ndof DOFs (thread 0).  Tiles (bi, bj), bi <= bj,
+// are numbered by column stripe of `stripe` tile columns [c0, c1), then by
+// row bi, then by column bj, so that the CTAs running at one time read the
+// rows of one stripe and its columns: the stripe's columns (sized to stay in
+// L2) are read from DRAM once, instead of every row block streaming all its
+// columns through L2.  A stripe of ntile columns is the row-major order.
 template <int R>
-__device__ void decode_all_pairs_tile(uint64_t id, uint64_t ntile, uint32_t ndof, uint32_t *rows,
-                                      uint32_t *cols, uint64_t *outs) {
-  uint64_t bi = 0;
+__device__ void decode_all_pairs_tile(uint64_t id, uint64_t ntile, uint64_t stripe, uint32_t ndof,
+                                      uint32_t *rows, uint32_t *cols, uint64_t *outs) {
+  uint64_t c0 = 0, w = 0;
   while (true) {
-    const uint64_t rowlen = ntile - bi;
-    if (id < rowlen) break;
-    id -= rowlen;
-    ++bi;
+    w = min(ntile, c0 + stripe) - c0;
+    const uint64_t cnt = c0 * w + w * (w + 1) / 2;   // full rows above c0, then the triangle
+    if (id < cnt) break;
+    id -= cnt;
+    c0 += w;
   }
-  const uint64_t bj = bi + id;
+  uint64_t bi, bj;
+  if (id < c0 * w) {
+    bi = id / w;
+    bj = c0 + id % w;
+  } else {
+    id -= c0 * w;
+    uint64_t r = 0;   // triangle row r (DOF block c0 + r) holds w - r tiles
+    while (id >= w - r) {
+      id -= w - r;
+      ++r;
+    }
+    bi = c0 + r;
+    bj = bi + id;
+  }
   for (int r = 0; r < R; ++r) {
     const uint64_t i = bi * R + r;
     rows[r] = (uint32_t)(i < ndof ? i : bi * R);
@@ -680,7 +699,7 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
   const int tid = threadIdx.x;
   if (tid == 0) {
     if (P.all_pairs) {
-      decode_all_pairs_tile<R>(blockIdx.x, P.ntile, P.ndof, rows_s, cols_s, out_s);
+      decode_all_pairs_tile<R>(blockIdx.x, P.ntile, P.stripe, P.ndof, rows_s, cols_s, out_s);
     } else {
       const PairTask &tk = tasks[blockIdx.x];
       for (int r = 0; r < R; ++r) rows_s[r] = tk.rows[r < tk.nr ? r : 0];
@@ -741,7 +760,8 @@ pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nit
       }
       const int s = lo;
       sys_s = s;
-      decode_all_pairs_tile<R>(item - sys[s].item_begin, sys[s].ntile, sys[s].ndof, rows_s,
+      decode_all_pairs_tile<R>(item - sys[s].item_begin, sys[s].ntile, sys[s].stripe, sys[s].ndof,
+                               rows_s,
                                cols_s, out_s);
     }
     __syncthreads();
@@ -1024,6 +1044,14 @@ entropy2d_counts_kernel(const uint32_t *__restrict__ pairs, const uint8_t *__res
 }
 
 // ----------------------------------------------------------------------------
+uint64_t all_pairs_stripe(int tile, uint64_t nframes, uint64_t ntile) {
+  // the columns of a stripe (tile DOFs per tile column, nframes bytes each)
+  // take at most kStripeBytes of L2
+  constexpr uint64_t kStripeBytes = 48ull << 20;
+  const uint64_t per = (uint64_t)std::max(tile, 1) * std::max<uint64_t>(nframes, 1);
+  return std::max<uint64_t>(1, std::min<uint64_t>(ntile, kStripeBytes / per));
+}
+
 int moment_scale(uint64_t n) {
   if (n < 3) return 52;
   const double L = (double)n * std::log((double)n);   // largest possible moment
@@ -1205,22 +1233,24 @@ int launch_pairs_atomic(centre_ctx *ctx, const PairParams &P, const PairTask *d_
   if (ntasks == 0) return CENTRE_OK;
   if ((uint64_t)P.ndof * P.nschemes * P.nframes >= kMaxHistBinBytes)
     return set_error(ctx, CENTRE_E_ARG, "bin matrix of 16 GiB or more (histogram counts)");
+  PairParams Q = P;
+  if (Q.all_pairs) Q.stripe = all_pairs_stripe(Q.tile, Q.nframes, Q.ntile);
   KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
   int rc;
-  if (P.all_pairs) {
-    switch (P.tile) {
-      case 4: rc = launch_hist<4, 4>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
-      case 3: rc = launch_hist<3, 3>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
-      case 2: rc = launch_hist<2, 2>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
-      default: rc = launch_hist<1, 1>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
+  if (Q.all_pairs) {
+    switch (Q.tile) {
+      case 4: rc = launch_hist<4, 4>(ctx, Q, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
+      case 3: rc = launch_hist<3, 3>(ctx, Q, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
+      case 2: rc = launch_hist<2, 2>(ctx, Q, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
+      default: rc = launch_hist<1, 1>(ctx, Q, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts); break;
     }
   } else {
-    const int w = pair_tile_for(P.nb);
-    if (w >= 16) rc = launch_hist<1, 16>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
-    else if (w >= 8) rc = launch_hist<1, 8>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
-    else if (w >= 4) rc = launch_hist<1, 4>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
-    else if (w >= 2) rc = launch_hist<1, 2>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
-    else rc = launch_hist<1, 1>(ctx, P, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
+    const int w = pair_tile_for(Q.nb);
+    if (w >= 16) rc = launch_hist<1, 16>(ctx, Q, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
+    else if (w >= 8) rc = launch_hist<1, 8>(ctx, Q, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
+    else if (w >= 4) rc = launch_hist<1, 4>(ctx, Q, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
+    else if (w >= 2) rc = launch_hist<1, 2>(ctx, Q, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
+    else rc = launch_hist<1, 1>(ctx, Q, d_tasks, ntasks, d_fix, d_sclnc, d_nnz, d_counts);
   }
   ctx->launches++;
   if (rc != CENTRE_OK) return rc;

@@ -39,6 +39,7 @@ struct BatchSys {
   uint64_t nframes;
   uint64_t step_size;
   uint64_t ntile;        // tiles per side of the all-pairs grid
+  uint64_t stripe;       // tile columns per stripe of the tile order
   uint64_t item_begin;   // first work item of this trajectory
   uint32_t ndof;
   unsigned long long *sclnc;
@@ -59,6 +60,8 @@ struct PairParams {
   uint64_t nframes;
   uint64_t step_size;
   uint64_t ntile;       // tiles per side (all-pairs mode)
+  uint64_t stripe;      // tile columns per stripe of the tile order (all-pairs
+                        // mode; set by launch_pairs_atomic)
   uint32_t ndof;
   int nschemes;
   int scheme;
@@ -116,6 +119,9 @@ __device__ __forceinline__ void tri_pair(uint64_t p, uint64_t n, uint32_t &i, ui
   j = (uint32_t)(p - start(r) + (uint64_t)r + 1);
 }
 
+// Tile columns per stripe of the all-pairs tile order (decode_all_pairs_tile)
+// for tiles of `tile` DOFs per side and nframes bytes per DOF row.
+uint64_t all_pairs_stripe(int tile, uint64_t nframes, uint64_t ntile);
 // Moment scale for n frames used (see clnc_fix).
 int moment_scale(uint64_t n);
 // Fills tab[c] = F(c) for c < kTabGlobal at scale s (one kernel launch on

@@ -443,25 +443,40 @@ def test_tc_counts_many_tiles_per_cta(gpu, orc, natoms, nframes, nsteps, nb):
 
 
 # ----------------------------------------------------- von Mises KDE ----
+# Frames per torsion whose conformer may differ from the oracle's: only a
+# frame within rounding (1e-9 rad) of a minimum can fall on either side, and
+# a float32 torsion lies that close to a given double minimum with
+# probability ~1e-2 per float value it takes, so more than one such frame in
+# a torsion means the minima or the assignment disagree.
+KDE_MAX_DIFF_FRAMES = 1
+
+
 def _kde_compare(gb, gm, gf, ob, omins, of, x):
-    """Bins equal except frames within rounding of a minimum; minima agree."""
+    """Bins equal except frames within rounding of a minimum (at most
+    KDE_MAX_DIFF_FRAMES per torsion); minima agree.  Returns the number of
+    differing frames."""
     assert gf == of
     np.testing.assert_allclose(gm[:gf], omins, rtol=0, atol=1e-9)
     diff = np.nonzero(gb != ob)[0]
     for k in diff:
         assert np.min(np.abs(np.float64(x[k]) - omins)) < 1e-9, (k, x[k])
+    assert len(diff) <= KDE_MAX_DIFF_FRAMES, len(diff)
     return len(diff)
 
 
 def test_vmkde_golden_fixture(gpu, golden):
     g = golden("vmkde_ref.npz")
     t = g["torsions"]
+    ndiff = 0
     for kappa in (1.0, 8.0):
         bins, mins, nf = gpu.discretize_vmkde(t, 5, kappa, 5, 1e-4, 1000)
         for d in range(len(t)):
             want_b = g[f"k{kappa:g}_d{d}_bins"]
             want_m = g[f"k{kappa:g}_d{d}_minima"]
-            _kde_compare(bins[d, 0], mins[d], int(nf[d]), want_b, want_m, len(want_m), t[d])
+            ndiff += _kde_compare(bins[d, 0], mins[d], int(nf[d]), want_b, want_m, len(want_m),
+                                  t[d])
+    print(f"KDE frames differing from the reference fixture: {ndiff} of "
+          f"{2 * t.shape[0] * t.shape[1]}")
 
 
 @pytest.mark.parametrize("nframes,kappa,nconf", [(20_000, 1.0, 5), (10_007, 8.0, 3), (4_000, 50.0, 9)])
@@ -469,6 +484,8 @@ def test_vmkde_vs_oracle(gpu, orc, nframes, kappa, nconf):
     tr = chain_trajectory(12, nframes, seed=int(kappa) + nframes)
     t = tr.torsions
     bins, mins, nf = gpu.discretize_vmkde(t, nconf, kappa, 5, 1e-4, 1000)
+    ndiff = 0
     for d in range(len(t)):
         ob, om, of = orc.vmkde(t[d], nconf, kappa, 5, 1e-4, 1000)
-        _kde_compare(bins[d, 0], mins[d], int(nf[d]), ob, om, of, t[d])
+        ndiff += _kde_compare(bins[d, 0], mins[d], int(nf[d]), ob, om, of, t[d])
+    print(f"KDE frames differing from the oracle: {ndiff} of {t.size}")

@@ -129,6 +129,37 @@ def test_pipeline_all_pairs(gpu, tmp_path):
                     assert row[4] == f"{res['mi'][q].reshape(-1)[g]:.6f}"
 
 
+def test_pipeline_multiple_bat_files(gpu, tmp_path):
+    """Several BAT files listed in discretization.fname are read in order and
+    their frames concatenated (src/Inputs.cpp:555-625): a trajectory split
+    into two files gives the same bin files, entropy contributions and CSVs,
+    byte for byte, as the whole trajectory in one file."""
+    tr = chain_trajectory(10, 6001, seed=31)
+    body = BODY.replace("fname = traj_bat.nc", "fname = part1_bat.nc, part2_bat.nc")
+    single = tmp_path / "single"
+    single.mkdir()
+    out1 = case(single, tr, BODY)
+    split = tmp_path / "split"
+    split.mkdir()
+    (split / "out").mkdir()
+    cut = 2500
+    cdf5.write_bat(str(split / "part1_bat.nc"), tr.bonds[:, :cut], tr.angles[:, :cut],
+                   tr.torsions[:, :cut])
+    cdf5.write_bat(str(split / "part2_bat.nc"), tr.bonds[:, cut:], tr.angles[:, cut:],
+                   tr.torsions[:, cut:])
+    cfg = split / "in.cfg"
+    cfg.write_text(f"[control]\n    infilepath = {split}/\n    outfilepath = {split}/out/\n" + body)
+    r = subprocess.run([TOOL, "-i", str(cfg), "-O"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out2 = split / "out"
+    names = sorted(f for f in os.listdir(out1) if f.endswith((".nc", ".csv")))
+    assert any(f.startswith("bin_") for f in names) and any(f.startswith("entcontri_") for f in names)
+    assert any(f.startswith("MIST-") for f in names)
+    assert names == sorted(f for f in os.listdir(out2) if f.endswith((".nc", ".csv")))
+    for f in names:
+        assert open(out1 / f, "rb").read() == open(out2 / f, "rb").read(), f
+
+
 def test_pipeline_subset_neighbours_and_frames(gpu, tmp_path):
     tr = chain_trajectory(11, 5003, seed=22)
     (tmp_path / "sub.txt").write_text("bond 10 3 0 2 5;\nangle 9 2 1 4;\ntorsion 8 4 0 1 2 6;\n")
