@@ -139,6 +139,8 @@ _SIGS = {
                                       C.c_uint64, _vp, _vp]),
     "centre_gpu_pair_moments": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp,
                                           C.c_int, _vp, _vp, _vp]),
+    "centre_gpu_corr_gemm_dev": (C.c_int, [_vp, _vp, C.c_uint32, C.c_uint32, C.c_uint32, _vp,
+                                           C.c_uint32]),
     "centre_gpu_score": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp, _vp,
                                    C.c_uint64, _vp, _vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     "centre_gpu_score_dev": (C.c_int, [_vp, C.POINTER(EntropyParams), C.c_uint32, _vp, _vp,

@@ -206,6 +206,12 @@ class Context:
                                                   C.byref(scale)))
         return clnc, nnz, scale.value
 
+    def corr_gemm_dev(self, X, n, K, ldx, R, ldr):
+        """R = X X^T on the tensor cores (X: CUDA bf16 [n][ldx], R: CUDA
+        float32 [n][ldr])."""
+        self.check(self.L.centre_gpu_corr_gemm_dev(self.h, _ptr(X), int(n), int(K), int(ldx),
+                                                   _ptr(R), int(ldr)))
+
     def score(self, params: EntropyParams, types, s1, s2, pairs=None, build_tree=True,
               want_mi=True, mi_out=None):
         types = _c(types, np.uint8)

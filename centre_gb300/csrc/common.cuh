@@ -53,7 +53,6 @@ struct centre_ctx {
   double timer_ms[4] = {0, 0, 0, 0};
   uint64_t timer_n[4] = {0, 0, 0, 0};
   void *batch_state = nullptr;  // tuned tiles and the cached batch graph
-  void *cublas = nullptr;       // cuBLAS handle of the pair screen's correlation GEMM
 };
 
 namespace centre {

@@ -9,7 +9,8 @@
 //   1. per-DOF columns over the first nframes/feat_div frames: a torsion
 //      gives (cos, sin) of its bin-centre angle, a bond or angle its bin
 //      index; each column standardised, stored bf16 DOF-major;
-//   2. their correlation matrix R = X^T X / F (one bf16 GEMM, cuBLAS);
+//   2. their correlation matrix R = X X^T (X standardised and scaled by
+//      1/sqrt(F): one bf16 GEMM on the tensor cores, gemm_tc.cu);
 //   3. per DOF, the nprefilter partners with the largest squared Frobenius
 //      norm of their 2x2 correlation block (radix select in shared memory);
 //   4. a BF16 MLP 12 -> 64 -> 64 -> 1 (ReLU) scores those partners from 12
@@ -22,7 +23,6 @@
 // step), by hand-written forward, backward and Adam kernels.  Exact MI of
 // the selected pairs (centre_gpu_entropy2d_dev) remains the judge; the
 // caller compares against all pairs when it wants the error.
-#include <cublas_v2.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -116,11 +116,13 @@ __global__ void column_stats_kernel(const uint8_t *__restrict__ bins, const uint
   }
 }
 
-// X [2*ndof][F] bf16, DOF-major: column 2d = u, 2d+1 = v, standardised and
-// scaled by 1/sqrt(F) so that X X^T is the correlation matrix.
+// X [2*ndof][ldx] bf16, DOF-major: row 2d = u, 2d+1 = v over the F frames,
+// standardised and scaled by 1/sqrt(F) so that X X^T is the correlation
+// matrix (ldx >= F; the GEMM reads nothing past F).
 __global__ void columns_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ types,
                                uint64_t nframes, int nschemes, uint32_t F, int nb,
-                               const float *__restrict__ stats, __nv_bfloat16 *__restrict__ X) {
+                               const float *__restrict__ stats, uint32_t ldx,
+                               __nv_bfloat16 *__restrict__ X) {
   const uint32_t d = blockIdx.y;
   const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= F) return;
@@ -133,28 +135,30 @@ __global__ void columns_kernel(const uint8_t *__restrict__ bins, const uint8_t *
     v = 0.f;
   }
   const float s = rsqrtf((float)F);
-  X[(uint64_t)(2 * d) * F + f] = __float2bfloat16_rn((u - stats[d * 4]) * stats[d * 4 + 1] * s);
-  X[(uint64_t)(2 * d + 1) * F + f] = __float2bfloat16_rn((v - stats[d * 4 + 2]) * stats[d * 4 + 3] * s);
+  X[(uint64_t)(2 * d) * ldx + f] = __float2bfloat16_rn((u - stats[d * 4]) * stats[d * 4 + 1] * s);
+  X[(uint64_t)(2 * d + 1) * ldx + f] =
+      __float2bfloat16_rn((v - stats[d * 4 + 2]) * stats[d * 4 + 3] * s);
 }
 
 // ------------------------------------------------------------ features ---
 struct FeatCtx {
-  const float *R;        // [2D][2D] column-major, ld = 2D
+  const float *R;        // [2D][ld], symmetric
   const float *s1p;      // prefix entropy per DOF
   const uint8_t *types;
   const uint32_t *tid;   // index within its type
   uint32_t ndof;
+  uint32_t ld;           // R's leading dimension (>= 2D)
 };
 
 __device__ __forceinline__ float block_frob2(const FeatCtx &F, uint32_t i, uint32_t j) {
-  const uint64_t ld = 2ull * F.ndof;
+  const uint64_t ld = F.ld;
   const float a = F.R[(2ull * j) + (2ull * i) * ld], b = F.R[(2ull * j + 1) + (2ull * i) * ld];
   const float c = F.R[(2ull * j) + (2ull * i + 1) * ld], e = F.R[(2ull * j + 1) + (2ull * i + 1) * ld];
   return a * a + b * b + c * c + e * e;
 }
 
 __device__ void pair_features(const FeatCtx &F, uint32_t i, uint32_t j, float *f) {
-  const uint64_t ld = 2ull * F.ndof;
+  const uint64_t ld = F.ld;
   const float ruu = F.R[(2ull * j) + (2ull * i) * ld];
   const float rvu = F.R[(2ull * j + 1) + (2ull * i) * ld];
   const float ruv = F.R[(2ull * j) + (2ull * i + 1) * ld];
@@ -546,10 +550,7 @@ double uniform01(uint64_t &s) { return (double)(splitmix(s) >> 11) * (1.0 / 9007
 
 }  // namespace
 
-void screen_state_free(centre_ctx *ctx) {
-  if (ctx->cublas) cublasDestroy((cublasHandle_t)ctx->cublas);
-  ctx->cublas = nullptr;
-}
+void screen_state_free(centre_ctx *) {}
 
 // He-uniform initial weights, zero biases (host, seeded).
 void screen_init_weights(uint64_t seed, float *w) {
@@ -657,36 +658,24 @@ extern "C" int centre_gpu_screen_dev(centre_ctx *ctx, const centre_entropy_param
   CENTRE_TRY(dalloc(ctx, s1p, sizeof(float) * D));
   CENTRE_TRY(dalloc(ctx, dtid, sizeof(uint32_t) * D));
   CENTRE_TRY(dalloc(ctx, stats, sizeof(float) * D * 4));
-  CENTRE_TRY(dalloc(ctx, X, sizeof(__nv_bfloat16) * 2ull * D * F));
-  CENTRE_TRY(dalloc(ctx, R, sizeof(float) * 4ull * D * D));
+  // row strides the tensor-core GEMM takes: X rows 16-byte aligned, R rows
+  // of whole float4s
+  const uint32_t ldx = (F + 7u) & ~7u, ldr = (2 * D + 3u) & ~3u;
+  CENTRE_TRY(dalloc(ctx, X, sizeof(__nv_bfloat16) * 2ull * D * ldx));
+  CENTRE_TRY(dalloc(ctx, R, sizeof(float) * 2ull * D * ldr));
   CENTRE_CUDA(ctx, cudaMemcpyAsync(dtid.p, tid.data(), sizeof(uint32_t) * D, cudaMemcpyHostToDevice, st));
   int rc = centre_gpu_entropy1d_dev(ctx, &pl, D, types, bins, extremes, (double *)s1l.p, nullptr);
   if (rc != CENTRE_OK) return rc;
   gather_s1_kernel<<<(D + 255) / 256, 256, 0, st>>>((double *)s1l.p, D, Gl, (float *)s1p.p);
   column_stats_kernel<<<D, 256, 0, st>>>(bins, types, p->nframes, p->nschemes, F, nb, (float *)stats.p);
   columns_kernel<<<dim3((F + 255) / 256, D), 256, 0, st>>>(bins, types, p->nframes, p->nschemes, F,
-                                                           nb, (float *)stats.p,
+                                                           nb, (float *)stats.p, ldx,
                                                            (__nv_bfloat16 *)X.p);
   ctx->launches += 3;
   CENTRE_CUDA(ctx, cudaGetLastError());
-  // R = X X^T: X is column-major (F x 2D), ld F
-  {
-    if (!ctx->cublas) {
-      cublasHandle_t h;
-      if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS)
-        return set_error(ctx, CENTRE_E_CUDA, "screen: cublasCreate failed");
-      ctx->cublas = (void *)h;
-    }
-    cublasHandle_t h = (cublasHandle_t)ctx->cublas;
-    cublasSetStream(h, st);
-    const float one = 1.f, zero = 0.f;
-    const int n2 = (int)(2 * D);
-    if (cublasGemmEx(h, CUBLAS_OP_T, CUBLAS_OP_N, n2, n2, (int)F, &one, X.p, CUDA_R_16BF, (int)F,
-                     X.p, CUDA_R_16BF, (int)F, &zero, R.p, CUDA_R_32F, n2, CUBLAS_COMPUTE_32F,
-                     CUBLAS_GEMM_DEFAULT) != CUBLAS_STATUS_SUCCESS)
-      return set_error(ctx, CENTRE_E_CUDA, "screen: correlation GEMM failed");
-  }
-  FeatCtx FC{(const float *)R.p, (const float *)s1p.p, types, (const uint32_t *)dtid.p, D};
+  // R = X X^T on the tensor cores (hand-written tcgen05 GEMM, gemm_tc.cu)
+  CENTRE_TRY(launch_corr_gemm(ctx, X.p, 2 * D, F, ldx, (float *)R.p, ldr));
+  FeatCtx FC{(const float *)R.p, (const float *)s1p.p, types, (const uint32_t *)dtid.p, D, ldr};
   // ---- training on exact MI of random pairs over the prefix -------------
   Buf w, wbf, m1, m2, g, ls;
   CENTRE_TRY(dalloc(ctx, w, sizeof(float) * kNParams));

@@ -221,6 +221,15 @@ int centre_gpu_counts2d(centre_ctx *ctx, const centre_entropy_params *p,
                         uint32_t ndof, const uint8_t *bins, uint64_t npairs,
                         const uint32_t *pairs, uint64_t *freq);
 
+/* The learned screen's correlation matrix on the tensor cores (no
+ * counterpart in the reference, which reads neighbour lists from files,
+ * src/Centre.cpp:459-593): R = X X^T for X, n rows of K bf16 values with
+ * leading dimension ldx (a multiple of 8, 16-byte aligned), into R, n rows
+ * of fp32 with leading dimension ldr (a multiple of 4).  Device pointers;
+ * returns when the GEMM has finished. */
+int centre_gpu_corr_gemm_dev(centre_ctx *ctx, const void *X, uint32_t n, uint32_t K,
+                             uint32_t ldx, float *R, uint32_t ldr);
+
 /* Integer moments of the joint counts of every pair i<j for one bin scheme,
  * as both count forms produce them (no reference counterpart: the
  * reference keeps the counts themselves, src/Estimators.cpp:130-205, and sums
