@@ -611,10 +611,27 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__
       nvalid = (int)(cur.f1 - cur.f0);
       load_lane_bins(P, sl, nmine, nvalid, cur.f0, lane, pb);
     }
-    uint64_t marked = ~0ull;     // tile of the chunk this warp last marked
+    // Fetch this warp's next chunk (kStages on); true when it lies in the
+    // same tile as the chunk just marked.
+    auto fetch = [&]() -> bool {
+      for (int i = 0; i < kStages; ++i) cur = walk.next();
+      if (!cur.valid) return false;
+      const bool same = cur.ti == tile;
+      if (!same) set_tile(cur.ti);
+      nvalid = (int)(cur.f1 - cur.f0);
+      load_lane_bins(P, sl, nmine, nvalid, cur.f0, lane, pb);
+      return same;
+    };
     uint32_t cph = 0;            // phase of S.cleared[p]
-    while (cur.valid) {
-      // wait until the MMA has consumed this stage's previous chunk
+    bool aborted = false;
+    // Outer loop: one pass per tile.  Its first chunk is marked here; when
+    // the stage comes from another tile, the other warps of this stage own
+    // rows this warp may have marked (and the reverse), so every warp of the
+    // stage clears its previous chunk before any sets the new one.  All
+    // warps of a stage walk the same chunks, so they all meet here.  The
+    // tile's other chunks are marked by the inner loop, which holds no
+    // barrier code (with it, the marking loop compiles to slower code).
+    while (cur.valid && !aborted) {
       int go = 1;
       if (lane == 0 && used) go = wait_bar(S, &S.empty[p], ph, flag) ? 1 : 0;
       go = __shfl_sync(0xffffffffu, go, 0);
@@ -622,14 +639,7 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__
       if (used) {
         ph ^= 1u;
         mark_clear(addr);
-      }
-      __syncwarp();
-      if (used && cur.ti != marked) {
-        // The stage moves to another tile, where the other warps of this
-        // stage own rows this warp may have marked (and the reverse): every
-        // warp of the stage clears its previous chunk before any sets the
-        // new one.  All warps of a stage walk the same chunks, so they all
-        // take this branch together.
+        __syncwarp();
         int ok = 1;
         if (lane == 0) {
           mbar_arrive(&S.cleared[p]);
@@ -638,19 +648,29 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__
         cph ^= 1u;
         ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) break;
-        __syncwarp();
       }
+      __syncwarp();
       mark_set(P, sl, nmine, edgemask, nvalid, sink, lane, pb, addr, flag);
-      marked = cur.ti;
       fence_proxy_async();
       mbar_arrive(&S.full[p]);
-      // fetch this warp's next chunk
       used = true;
-      for (int i = 0; i < kStages; ++i) cur = walk.next();
-      if (cur.valid) {
-        if (cur.ti != tile) set_tile(cur.ti);
-        nvalid = (int)(cur.f1 - cur.f0);
-        load_lane_bins(P, sl, nmine, nvalid, cur.f0, lane, pb);
+      bool more = fetch();
+      while (more) {
+        // wait until the MMA has consumed this stage's previous chunk
+        go = 1;
+        if (lane == 0) go = wait_bar(S, &S.empty[p], ph, flag) ? 1 : 0;
+        go = __shfl_sync(0xffffffffu, go, 0);
+        if (!go) {
+          aborted = true;
+          break;
+        }
+        ph ^= 1u;
+        mark_clear(addr);
+        __syncwarp();
+        mark_set(P, sl, nmine, edgemask, nvalid, sink, lane, pb, addr, flag);
+        fence_proxy_async();
+        mbar_arrive(&S.full[p]);
+        more = fetch();
       }
     }
   } else {
