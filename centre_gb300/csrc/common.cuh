@@ -36,7 +36,7 @@ struct centre_ctx {
   bool own_stream = false;
   uint64_t launches = 0;
   std::string last_error;
-  centre::DevBuf scratch[8];
+  centre::DevBuf scratch[9];   // one per ScratchSlot (below)
   int *d_flag = nullptr;   // device error flag (bin range, timeouts)
   int *h_flag = nullptr;   // pinned mirror
   int cc_major = 0, cc_minor = 0;
@@ -67,6 +67,7 @@ enum ScratchSlot {
   kSlotPairs = 5,
   kSlotAux2 = 6,
   kSlotAux3 = 7,
+  kSlotTcBins = 8,  // bins re-pitched for TMA (tensor-core counts)
 };
 
 int set_error(centre_ctx *ctx, int status, const std::string &msg);

@@ -178,6 +178,8 @@ int launch_gridkde(centre_ctx *ctx, int bat_type, const float *d_data, uint32_t 
 size_t gridkde_work_bytes(uint32_t ndof);
 int launch_df_exp_eval(centre_ctx *ctx, const double *d_y, uint64_t n, double *d_out);
 
+// gemm_tc.cu: the driver's cuTensorMapEncodeTiled (null when unavailable)
+void *tensor_map_encoder();
 // gemm_tc.cu: R = X X^T (X bf16 n x K, leading dimension ldx, a multiple of
 // 8; R fp32 n x n, leading dimension ldr, a multiple of 4)
 int launch_corr_gemm(centre_ctx *ctx, const void *X, uint32_t n, uint32_t K, uint32_t ldx,

@@ -332,9 +332,21 @@ corr_gemm_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant
 size_t gemm_smem_bytes() { return 1024 + (size_t)kStages * kStageBytes + sizeof(GemmSmem); }
 
 std::once_flag g_encode_once;
-PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+void *g_encode_fn = nullptr;
 
 }  // namespace
+
+void *tensor_map_encoder() {
+  std::call_once(g_encode_once, [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode_fn = fn;
+  });
+  return g_encode_fn;
+}
 
 int launch_corr_gemm(centre_ctx *ctx, const void *X, uint32_t n, uint32_t K, uint32_t ldx,
                      float *R, uint32_t ldr) {
@@ -342,14 +354,7 @@ int launch_corr_gemm(centre_ctx *ctx, const void *X, uint32_t n, uint32_t K, uin
   if (ldx % 8 != 0 || ldx < K || ldr % 4 != 0 || ldr < n ||
       (reinterpret_cast<uintptr_t>(X) & 15u) != 0 || (reinterpret_cast<uintptr_t>(R) & 15u) != 0)
     return set_error(ctx, CENTRE_E_ARG, "correlation GEMM: bad layout");
-  std::call_once(g_encode_once, [] {
-    void *fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  });
+  auto g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tensor_map_encoder());
   if (!g_encode) return set_error(ctx, CENTRE_E_CUDA, "cuTensorMapEncodeTiled unavailable");
   // X as a 2-D tensor: K elements per row (the inner dimension; loads past
   // it, and rows past n, read zeros), n rows, ldx elements apart; boxes of

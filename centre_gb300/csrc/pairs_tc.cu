@@ -6,42 +6,54 @@
 // entropy.cu for the factorisation).
 //
 // Formulation.  Rows of the one-hot matrix O are (DOF, bin) packed without
-// padding: row = dof * nb + bin.  O[frame][row] = 1 when DOF's bin at frame is
-// bin.  The joint counts of every pair are blocks of O^T O.  A CTA computes a
-// 128 x 256 tile of O^T O (rows [rb, rb+128), columns [cb, cb+256)) over all
-// frames with tcgen05.mma kind::f8f6f4 (E4M3 operands, FP32 accumulator in
-// TMEM): 1.0 and 0.0 are exact in E4M3 and FP32 sums of integers below 2^24
-// are exact, so the counts are exact.
+// padding: row = dof * nb + bin.  O[frame][row] = 2 when DOF's bin at frame is
+// bin, else 0.  The joint counts of every pair are blocks of O^T O / 4.  A CTA
+// computes a 128 x 256 tile of O^T O (rows [rb, rb+128), columns [cb,
+// cb+256)) over all frames with tcgen05.mma kind::f8f6f4 (E4M3 operands, FP32
+// accumulator in TMEM): 2.0 and 0.0 are exact in E4M3 and FP32 sums of
+// multiples of 4 up to 2^24 are exact, so the counts are exact for up to
+// 2^22 frames.
 //
-// Operand tiles stay zero in shared memory; producer warps write one E4M3 1.0
-// byte per (frame, DOF) into the K-major, 128-byte-swizzled tiles and clear
-// exactly those bytes again (at addresses kept in registers) once the MMA has
-// consumed the stage, so building a one-hot tile costs two byte stores per
-// (frame, DOF) instead of writing the whole tile.  Lane l of a producer warp
-// owns frames 4l..4l+3 of the chunk: its bins arrive in one coalesced 32-bit
-// load per DOF, and the stores of one instruction spread over the banks.
+// Operands.  The frame axis is cut into 128-frame blocks (one 128-byte
+// K-major row of an operand tile); a block that holds the end of a
+// convergence step is used twice, once per side of the step boundary (a
+// "piece" is a block and a frame range inside it).  A loader warp stages the
+// bins of the tile's DOFs for each piece with two TMA loads
+// (cp.async.bulk.tensor.2d: the 9 DOF rows of the A tile and the 17 of the B
+// tile, 128 frames each) into a six-deep ring.  Twelve producer warps then
+// rewrite the whole operand stage (128 + 256 rows x 128 bytes, 128-byte
+// swizzled) from those bins: lane (g, s) of warp w owns segment g (16 frames)
+// of the 8 rows 32w + 8s .. +7 of the stage, in every piece, so no producer
+// ever writes where another does and no stage needs clearing.  For each row
+// it compares the 16 bins of its DOF with the row's bin four at a time with
+// integer arithmetic (no per-byte work) and writes the 16 one-hot bytes with
+// one 128-bit shared store; the stores of one instruction hit the eight
+// 16-byte bank groups of a swizzled row group once each.  Frames of a piece's
+// block outside the piece are zeroed in the A operand only.
 //
-// Convergence steps are prefixes of the frame axis: K-chunks never straddle a
-// step boundary.  The MMAs of a step accumulate into TMEM columns [256, 512)
-// starting from zero; at the step's end the epilogue warps add them to the
-// cumulative counts in columns [0, 256) and release the accumulator at once,
-// so the next step's MMAs overlap the rest of the epilogue: reading the
-// cumulative counts (tcgen05.ld), reducing each (row DOF, column DOF) block to
-// sum F(c) (the 64-bit fixed-point c ln c of entropy.cuh) and the non-empty
-// cell count, and
+// Accumulation.  Convergence steps are prefixes of the frame axis.  The MMAs
+// of a step accumulate into TMEM columns [256, 512) starting from zero; at the
+// step's end the epilogue warps add them to the cumulative counts in columns
+// [0, 256) and release the accumulator at once, so the next step's MMAs
+// overlap the rest of the epilogue: reading the cumulative counts
+// (tcgen05.ld), reducing each (row DOF, column DOF) block to sum F(c) (the
+// 64-bit fixed-point c ln c of entropy.cuh) and the non-empty cell count, and
 // adding them into the pair's moments with integer atomics (tiles split pair
 // blocks; integer addition keeps the result independent of the split).
 //
-// Warp roles (672 threads): warp 0 allocates TMEM and one lane issues the
-// MMAs; warps 1-12 produce operand stages, three per stage (warp 1+p+4h marks
-// the DOF slots h, h+3, ... of stage p, from a per-tile slot table in shared
-// memory), so the four stages are built concurrently without cross-warp
-// barriers, each warp prefetching the bins of its next chunk into registers
-// while it marks the current one (the marking is bound by instruction issue
-// and latency; more warps hide it); warps 13-20 run the epilogue as two
-// quartets over the two column halves (TMEM lane group = warp % 4).  Every
-// mbarrier wait is bounded: on expiry the kernel sets an error flag, lets the
-// MMAs it issued drain (again bounded), frees its TMEM and returns.
+// Warp roles (704 threads): warp 0 allocates TMEM and one lane issues the
+// MMAs; one lane of warp 1 issues the TMA loads of the bins; warps 2-13
+// produce operand stages (four A row groups, eight B row groups); warps 14-21
+// run the epilogue as two quartets over the two column halves (TMEM lane group
+// = warp % 4).  Every mbarrier wait is bounded: on expiry the kernel sets an
+// error flag, lets the MMAs and loads it issued drain (again bounded), frees
+// its TMEM and returns.
+//
+// Bins outside [0, nb) never steer an address here (the operand stores go to
+// fixed places); a check pass ahead of the contraction reports them.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <vector>
 
@@ -53,7 +65,7 @@ namespace {
 
 constexpr int kTileM = 128;                 // A rows (row DOF bins)
 constexpr int kTileN = 256;                 // B rows (column DOF bins)
-constexpr int kChunk = 128;                 // frames per stage (one 128 B row)
+constexpr int kChunk = 128;                 // frames per block (one 128 B row)
 constexpr int kStages = 4;
 constexpr int kABytes = kTileM * kChunk;    // 16 KB
 constexpr int kBBytes = kTileN * kChunk;    // 32 KB
@@ -61,45 +73,40 @@ constexpr int kStageBytes = kABytes + kBBytes;
 constexpr int kMinBins = 16;                // DOF slots per tile bounded below
 constexpr int kMaxSlotsA = kTileM / kMinBins + 1;  // 9
 constexpr int kMaxSlotsB = kTileN / kMinBins + 1;  // 17
-constexpr int kMaxSlots = kMaxSlotsA + kMaxSlotsB;
-constexpr int kTabTc = 2048;                // fixed-point c ln c entries in shared memory
-#ifndef CENTRE_TC_PRODUCERS_PER_STAGE
-#define CENTRE_TC_PRODUCERS_PER_STAGE 3
-#endif
-// Producer warps p, p + kStages, ... fill stage p, each the DOF slots
-// congruent to its rank modulo kPerStage (the marking is issue-bound: more
-// warps hide its latency).
-constexpr int kPerStage = CENTRE_TC_PRODUCERS_PER_STAGE;
-constexpr int kProducerWarps = kStages * kPerStage;
-constexpr int kSlotsPerWarp = (kMaxSlots + kPerStage - 1) / kPerStage;
+constexpr int kBinRows = kMaxSlotsA + kMaxSlotsB;  // DOF rows staged per piece
+constexpr int kBinBytes = kBinRows * kChunk;       // 3,328
+constexpr int kBinStages = 8;
+constexpr int kTabTc = 512;                 // fixed-point c ln c entries in shared memory
+constexpr int kGroupsA = kTileM / 32;       // 32-row groups of the A operand
+constexpr int kRowGroups = (kTileM + kTileN) / 32;   // 32-row groups of a stage
+// Producer warps: a team of kPerTeam warps per operand stage, each warp
+// rewriting kGroupsPerWarp row groups of every piece its stage takes.
+constexpr int kPerTeam = 3;
+constexpr int kGroupsPerWarp = kRowGroups / kPerTeam;
+constexpr int kProducers = kStages * kPerTeam;
 // Epilogue: kEpiGroups warp quartets, quartet g reading accumulator columns
 // [g * kEpiCols, (g + 1) * kEpiCols) of all 128 rows (a warp reads the TMEM
 // lanes of its warp index modulo 4).
-#ifndef CENTRE_TC_EPI_GROUPS
-#define CENTRE_TC_EPI_GROUPS 2
-#endif
-constexpr int kEpiGroups = CENTRE_TC_EPI_GROUPS;
+constexpr int kEpiGroups = 2;
 constexpr int kEpiCols = kTileN / kEpiGroups;
 constexpr int kEpilogue = 128 * kEpiGroups;
-constexpr int kThreads = 32 * (1 + kProducerWarps + 4 * kEpiGroups);
-constexpr int kFramesPerLane = kChunk / 32;              // 4
+constexpr int kWarpMma = 0;
+constexpr int kWarpLoad = 1;
+constexpr int kWarpProd = 2;
+constexpr int kWarpEpi = kWarpProd + kProducers;
+constexpr int kThreads = 32 * (kWarpEpi + 4 * kEpiGroups);
 // TMEM columns: [0, 256) the cumulative counts of the current step, read by
 // the epilogue; [256, 512) the MMA accumulator of the step's own frames
 constexpr unsigned kTmemCols = 512;
 constexpr uint32_t kIncCol = 256;
 constexpr long long kWaitCycles = 20000000000ll;  // ~10 s at 2 GHz
-constexpr uint8_t kOne = 0x38;              // 1.0 in E4M3
 
 struct TcParams {
-  const uint8_t *bins;
   const uint2 *tiles;     // (row tile, column tile)
   uint64_t ntiles;
-  uint64_t nframes;
   uint64_t step_size;
   uint32_t ndof;
   uint32_t nrows;         // ndof * nb
-  int nschemes;
-  int scheme;
   int nb;
   int nsteps;
   int fix_scale;          // moment scale s (counts beyond the table)
@@ -112,34 +119,17 @@ struct StageMeta {
   int d0b, ndb;
 };
 
-// A producer warp's DOF slot of the current tile: the DOF's bins row
-// (element offset), the stage address of the slot's row 0 (tile row
-// `base` = row of the DOF's bin 0 relative to the tile, may be negative), and
-// the tile's row count.
-struct SlotInfo {
-  uint64_t src;
-  uint32_t tb;
-  int base;
-  int rows;
-  int pad;
-};
-
 struct Smem {
-  uint64_t full[kStages];
-  uint64_t empty[kStages];
-  // per stage: the producer warps of the stage have cleared their previous
-  // chunk's bytes (needed when the stage moves to another tile, where the
-  // warps' DOF slots cover other rows)
-  uint64_t cleared[kStages];
+  uint64_t full[kStages];      // operand stage built (all producer lanes)
+  uint64_t empty[kStages];     // operand stage consumed (MMA commit)
+  uint64_t bfull[kBinStages];  // bins of a piece landed (TMA bytes)
+  uint64_t bempty[kBinStages]; // bins of a piece read (all producer lanes)
   uint64_t accfull;
   uint64_t accempty;
   uint64_t drain;
   uint32_t tmem_base;
   int abort_flag;
   int ego[2];       // epilogue's per-snapshot go/abort decision
-  uint32_t sink;    // target of one-hot stores that fall outside a tile
-  // per producer warp, its DOF slots of the current tile (see SlotInfo)
-  SlotInfo slots[kProducerWarps][kSlotsPerWarp];
   __align__(16) unsigned long long tab[kTabTc];   // F(c), fixed-point c ln c
   // per (row DOF slot, column DOF slot) block of the tile: the sum of F over
   // its cells and the non-empty cell count, filled with shared-memory
@@ -177,10 +167,15 @@ __device__ __forceinline__ void red_shared_u32(uint32_t addr, unsigned v) {
   asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
 }
 // Bounded wait: false when the kernel is aborting (timeout here or elsewhere).
+// kSleepNs > 0 backs off between polls: for waits off the critical path
+// (the loader, the epilogue's step wait), whose polling would otherwise take
+// issue slots from the producers on the same scheduler.
+template <int kSleepNs = 0>
 __device__ bool wait_bar(Smem &S, uint64_t *bar, uint32_t parity, int *flag) {
   const long long t0 = clock64();
   uint32_t it = 0;
   while (!mbar_try_wait(bar, parity)) {
+    if (kSleepNs > 0) __nanosleep(kSleepNs);
     if (*(volatile int *)&S.abort_flag) return false;
     if ((++it & 255u) == 0 && clock64() - t0 > kWaitCycles) {
       atomicOr(flag, kFlagTimeout);
@@ -276,32 +271,92 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
                : "memory");
 }
 
-struct ChunkIter {
-  // walks (step, chunk) of the frame axis; chunks end at step boundaries
-  uint64_t ss;
-  int nsteps;
-  int t;
-  uint64_t f;     // next frame
-  uint64_t end;   // end of step t
-  __device__ void start(uint64_t step_size, int ns) {
-    ss = step_size;
-    nsteps = ns;
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// Bounded wait that ignores the abort flag: for copies the kernel issued,
+// which land whatever the other warps do.
+__device__ void wait_landed(uint64_t *bar, uint32_t parity, int *flag) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > kWaitCycles) {
+      atomicOr(flag, kFlagTimeout);
+      return;
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+      "%3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ uint4 lds128(uint32_t addr) {
+  uint4 v;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "r"(addr)
+               : "memory");
+  return v;
+}
+
+// The pieces of a CTA's work, in order: its tiles (first, first + stride,
+// ...), each over the convergence steps, each step over the 128-frame blocks
+// it touches.  Step t adds frames [t * step_size, (t + 1) * step_size); a
+// block that holds a step boundary is visited once per side of it.
+struct Piece {
+  uint32_t ti;      // tile index
+  uint32_t blk;     // block: frames [blk * 128, blk * 128 + 128)
+  int lo, hi;       // the piece's frames within the block
+  bool last;        // closes a convergence step
+  bool valid;
+};
+
+// (32-bit state: at most 2^22 frames, fewer than 2^32 tiles)
+struct PieceWalker {
+  uint32_t ti, stride, ntiles, ss, f, end;
+  int t, nsteps;
+  __device__ void start(uint32_t first, uint32_t stride_, uint32_t ntiles_, uint32_t ss_,
+                        int nsteps_) {
+    ti = first;
+    stride = stride_;
+    ntiles = ntiles_;
+    ss = ss_;
+    nsteps = nsteps_;
     t = 0;
     f = 0;
-    end = step_size;
+    end = ss_;
   }
-  // returns false when done; sets [f0, f1) and whether it closes a step
-  __device__ bool next(uint64_t &f0, uint64_t &f1, bool &last_of_step) {
-    if (t >= nsteps) return false;
-    f0 = f;
-    f1 = min(end, f0 + (uint64_t)kChunk);
-    last_of_step = (f1 == end);
-    f = f1;
-    if (last_of_step) {
-      ++t;
-      end += ss;
+  __device__ Piece next() {
+    Piece p;
+    p.valid = false;
+    while (ti < ntiles) {
+      if (t < nsteps) {
+        const uint32_t blk = f / kChunk;
+        const uint32_t hi = min(end, (blk + 1) * kChunk);
+        p.ti = ti;
+        p.blk = blk;
+        p.lo = (int)(f - blk * kChunk);
+        p.hi = (int)(hi - blk * kChunk);
+        p.last = hi == end;
+        p.valid = true;
+        f = hi;
+        if (p.last) {
+          ++t;
+          end += ss;
+        }
+        return p;
+      }
+      ti += stride;
+      t = 0;
+      f = 0;
+      end = ss;
     }
-    return true;
+    return p;
   }
 };
 
@@ -316,171 +371,97 @@ __device__ __forceinline__ void tile_geometry(const TcParams &P, uint2 tl, Stage
   m.ndb = lastb / P.nb - m.d0b + 1;
 }
 
-// Chunk c of a CTA's work: tile and frame range.  Walks the per-tile chunk
-// sequence (steps x 128-frame chunks, a chunk never straddles a step).
-struct ChunkPos {
-  uint64_t ti;      // tile index (global)
-  uint64_t f0, f1;
-  bool last;        // closes a convergence step
-  bool valid;
-};
-
-struct ChunkWalker {
-  uint64_t ti;
-  ChunkIter it;
-  uint64_t stride;
-  uint64_t ntiles;
-  __device__ void start(uint64_t first, uint64_t stride_, uint64_t ntiles_, uint64_t ss, int ns) {
-    ti = first;
-    stride = stride_;
-    ntiles = ntiles_;
-    it.start(ss, ns);
-  }
-  __device__ ChunkPos next() {
-    ChunkPos p;
-    p.valid = false;
-    while (ti < ntiles) {
-      if (it.next(p.f0, p.f1, p.last)) {
-        p.ti = ti;
-        p.valid = true;
-        return p;
-      }
-      ti += stride;
-      it.start(it.ss, it.nsteps);
-    }
-    return p;
-  }
-};
-
-// Slot geometry of a stage: DOF slot -> (A or B tile, first row of the DOF's
-// bins relative to the tile).
-__device__ __forceinline__ void slot_info(const TcParams &P, const StageMeta &m, int slot,
-                                          bool &isA, int &dof, int &base) {
-  isA = slot < m.nda;
-  dof = isA ? m.d0a + slot : m.d0b + (slot - m.nda);
-  base = dof * P.nb - (isA ? m.rb : m.cb);
-}
-
 // F(c) for counts beyond the global table (rare).  Kept out of line so the
 // unrolled epilogue loop stays small.
 __device__ __noinline__ unsigned long long clnc_far(unsigned c, int s) { return clnc_fix(c, s); }
 
-// Load the lane's 4 frames (4*lane .. +3 of the chunk) of the warp's DOF
-// slots into registers.  The values are first used one chunk later
-// (prefetch); the range check happens when they are marked.
-__device__ __forceinline__ void load_lane_bins(const TcParams &P, const SlotInfo *sl, int nmine,
-                                               int nvalid, uint64_t f0, int lane,
-                                               uint32_t (&pb)[kSlotsPerWarp]) {
-  const int k0 = kFramesPerLane * lane;
-  const int avail = max(0, min(kFramesPerLane, nvalid - k0));
+// One-hot of four frames: byte q of the result is 0x40 (E4M3 2.0) where byte
+// q of w (a bin) equals the row's bin (every byte of bb), else 0.  With x =
+// w ^ bb the byte is zero exactly on a match:
+//   bins < 64:  0xC0 - x lies in [0x81, 0xC0] and has bit 6 set only for x = 0;
+//   bins < 128: 0x80 - x lies in [0x01, 0x80] and has bit 7 set only for x = 0;
+//   otherwise:  (x & 0x7F) + 0x7F has bit 7 set iff the low 7 bits are not all
+//               zero, and x's own bit 7 covers the rest.
+// No byte borrows from or carries into its neighbour in any of the three.
+template <int kMode>
+__device__ __forceinline__ uint32_t onehot4(uint32_t w, uint32_t bb) {
+  const uint32_t x = w ^ bb;
+  if (kMode == 0) return (0xC0C0C0C0u - x) & 0x40404040u;
+  if (kMode == 1) return ((0x80808080u - x) >> 1) & 0x40404040u;
+  const uint32_t t = (x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
+  return (~(t | x) & 0x80808080u) >> 1;
+}
+
+// Byte mask of frames [a, b) among the four frames 0..3 of a word.
+__device__ __forceinline__ uint32_t frame_mask(int a, int b) {
+  a = min(max(a, 0), 4);
+  b = min(max(b, 0), 4);
+  return (uint32_t)(0xFFFFFFFFull << (8 * a)) & (uint32_t)~(0xFFFFFFFFull << (8 * b));
+}
+
+// The lane's 8 rows of one piece: row i (tile row rowbase + i) is the bin
+// bin0 + i of the DOF whose bins are wc, or, from row `split` on when the rows
+// cross into the next DOF, bin i - split of the DOF whose bins are wn.  The
+// rows' segment g lands at byte 128 i + 16 (g ^ i) of the 1024-byte row
+// group (the 128-byte swizzle, with rowbase a multiple of 8).
+template <int kMode, bool kSplit, bool kMask>
+__device__ __forceinline__ void build_rows(uint8_t *group, uint32_t g16, const uint4 &wc,
+                                           const uint4 &wn, int bin0, int split, int nb,
+                                           const uint32_t (&fm)[4]) {
 #pragma unroll
-  for (int i = 0; i < kSlotsPerWarp; ++i) {
-    uint32_t w = 0;
-    if (i < nmine && avail > 0) {
-      const uint8_t *src = P.bins + sl[i].src + f0 + k0;
-      if (avail == kFramesPerLane && ((reinterpret_cast<uintptr_t>(src) & 3u) == 0)) {
-        w = __ldg(reinterpret_cast<const uint32_t *>(src));
-      } else {
-#pragma unroll
-        for (int q = 0; q < kFramesPerLane; ++q)
-          if (q < avail) w |= (uint32_t)__ldg(src + q) << (8 * q);
-      }
+  for (int i = 0; i < 8; ++i) {
+    uint4 w = wc;
+    int b = bin0 + i;
+    if (kSplit && i >= split) {
+      w = wn;
+      b -= nb;
     }
-    pb[i] = w;
+    const uint32_t bb = (uint32_t)b * 0x01010101u;
+    uint4 o;
+    o.x = onehot4<kMode>(w.x, bb);
+    o.y = onehot4<kMode>(w.y, bb);
+    o.z = onehot4<kMode>(w.z, bb);
+    o.w = onehot4<kMode>(w.w, bb);
+    if (kMask) {
+      o.x &= fm[0];
+      o.y &= fm[1];
+      o.z &= fm[2];
+      o.w &= fm[3];
+    }
+    *reinterpret_cast<uint4 *>(group + (((uint32_t)i << 7) | (g16 ^ ((uint32_t)i << 4)))) = o;
   }
 }
 
-__device__ __forceinline__ void sts_u8(uint32_t addr, uint32_t v) {
-  asm volatile("st.shared.u8 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
-}
-
-// Set the one-hot bytes (E4M3 1.0) of the lane's frames and remember their
-// addresses for clearing.  In a K-major 128B-swizzled tile, element (row, k)
-// sits at (row << 7) + ((((k >> 4) ^ row) & 7) << 4) + (k & 15).  Positions
-// outside the tile (first/last DOF of a tile cut by its edge, frames past
-// the chunk's end) go to a scratch byte instead, so that clearing is one
-// unconditional store per position.  Slots whose DOF lies inside the tile
-// take the path without those checks when the chunk is full.
-constexpr int kLaneMarks = kSlotsPerWarp * kFramesPerLane;
-
-__device__ __forceinline__ void mark_set(const TcParams &P, const SlotInfo *sl, int nmine,
-                                         uint32_t edgemask, int nvalid, uint32_t sink, int lane,
-                                         uint32_t (&pb)[kSlotsPerWarp],
-                                         uint32_t (&addr)[kLaneMarks], int *flag) {
-  const int k0 = kFramesPerLane * lane;
-  const uint32_t g = (uint32_t)(k0 >> 4);
-  const uint32_t q0 = (uint32_t)(k0 & 15);
-  const int kv = nvalid - k0;
-  const bool full = nvalid == kChunk;
-#pragma unroll
-  for (int i = 0; i < kSlotsPerWarp; ++i) {
-    if (i < nmine) {
-      const int base = sl[i].base;
-      const uint32_t tbq = sl[i].tb + q0;
-      if (__vcmpgeu4(pb[i], 0x01010101u * (uint32_t)P.nb)) {
-        // a bin >= nb: report it and keep every store inside the tile
-        atomicOr(flag, kFlagBinRange);
-        pb[i] = 0;
-      }
-      if (full && !((edgemask >> i) & 1u)) {
-#pragma unroll
-        for (int q = 0; q < kFramesPerLane; ++q) {
-          const uint32_t b = (pb[i] >> (8 * q)) & 255u;
-          const uint32_t row = (uint32_t)base + b;
-          addr[i * kFramesPerLane + q] = tbq + (b << 7) + (((g ^ row) & 7u) << 4) + q;
-        }
-      } else {
-        const uint32_t rows = (uint32_t)sl[i].rows;
-#pragma unroll
-        for (int q = 0; q < kFramesPerLane; ++q) {
-          const uint32_t b = (pb[i] >> (8 * q)) & 255u;
-          const uint32_t row = (uint32_t)base + b;
-          const uint32_t a = tbq + (b << 7) + (((g ^ row) & 7u) << 4) + q;
-          addr[i * kFramesPerLane + q] = (row < rows && q < kv) ? a : sink;
-        }
-      }
-    } else {
-#pragma unroll
-      for (int q = 0; q < kFramesPerLane; ++q) addr[i * kFramesPerLane + q] = sink;
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < kLaneMarks; ++j) sts_u8(addr[j], kOne);
-}
-
-__device__ __forceinline__ void mark_clear(const uint32_t (&addr)[kLaneMarks]) {
-#pragma unroll
-  for (int j = 0; j < kLaneMarks; ++j) sts_u8(addr[j], 0u);
-}
-
-__global__ void __launch_bounds__(kThreads, 1)
-pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__restrict__ gfix,
+template <int kMode, bool kSplit>
+__global__ void __maxnreg__(80)
+pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                const __grid_constant__ TcParams P, const unsigned long long *__restrict__ gfix,
                 unsigned long long *__restrict__ sclnc, unsigned *__restrict__ nnz,
                 int *__restrict__ flag) {
   extern __shared__ __align__(1024) unsigned char dyn[];
-  // stages first (1024-aligned), then the bookkeeping block
+  // operand stages first (1024-aligned), then the bins ring, then the
+  // bookkeeping block
   const uint32_t pad = (1024u - (smem_u32(dyn) & 1023u)) & 1023u;
   uint8_t *stages = dyn + pad;
   const uint32_t stages_s = smem_u32(stages);
-  Smem &S = *reinterpret_cast<Smem *>(stages + kStages * kStageBytes);
+  const uint32_t bins_s = stages_s + (uint32_t)(kStages * kStageBytes);
+  Smem &S = *reinterpret_cast<Smem *>(stages + kStages * kStageBytes + kBinStages * kBinBytes);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   // ---- set-up ------------------------------------------------------------
-  {
-    uint4 z = make_uint4(0, 0, 0, 0);
-    uint4 *p = reinterpret_cast<uint4 *>(stages);
-    for (int i = tid; i < kStages * kStageBytes / 16; i += kThreads) p[i] = z;
-    for (int i = tid; i < kTabTc; i += kThreads) S.tab[i] = gfix[i];
-    for (int i = tid; i < kMaxSlotsA * kMaxSlotsB; i += kThreads) {
-      S.blk_x[i] = 0ull;
-      S.blk_nz[i] = 0u;
-    }
+  for (int i = tid; i < kTabTc; i += kThreads) S.tab[i] = gfix[i];
+  for (int i = tid; i < kMaxSlotsA * kMaxSlotsB; i += kThreads) {
+    S.blk_x[i] = 0ull;
+    S.blk_nz[i] = 0u;
   }
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&S.full[s], 32 * kPerStage);
+      mbar_init(&S.full[s], 32 * kPerTeam);
       mbar_init(&S.empty[s], 1);
-      mbar_init(&S.cleared[s], kPerStage);
+    }
+    for (int s = 0; s < kBinStages; ++s) {
+      mbar_init(&S.bfull[s], 1);
+      mbar_init(&S.bempty[s], 32 * kPerTeam);
     }
     mbar_init(&S.accfull, 1);
     mbar_init(&S.accempty, kEpilogue);
@@ -489,7 +470,7 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   fence_proxy_async();
-  if (warp == 0) {
+  if (warp == kWarpMma) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&S.tmem_base)),
                  "r"(kTmemCols)
@@ -501,183 +482,191 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__
   tc_fence_after();
   const uint32_t tmem = S.tmem_base;
 
-  if (warp == 0) {
+  if (warp == kWarpMma) {
     // ---- MMA issuer --------------------------------------------------------
     if (lane == 0) {
+      PieceWalker walk;
+      walk.start(blockIdx.x, gridDim.x, (uint32_t)P.ntiles, (uint32_t)P.step_size, P.nsteps);
       int s = 0;
-      uint32_t ph[kStages] = {};
+      uint32_t ph = 0;
       uint32_t nsnap = 0;
       bool issued = false;
-      bool ok = true;
-      for (uint64_t ti = blockIdx.x; ti < P.ntiles && ok; ti += gridDim.x) {
-        ChunkIter it;
-        it.start(P.step_size, P.nsteps);
-        uint64_t f0, f1;
-        bool last;
-        bool first = true;
-        while (ok && it.next(f0, f1, last)) {
-          if (!wait_bar(S, &S.full[s], ph[s], flag)) { ok = false; break; }
-          ph[s] ^= 1u;
+      bool first = true;
+      for (;;) {
+        const Piece pc = walk.next();
+        if (!pc.valid) break;
+        if (!wait_bar(S, &S.full[s], ph, flag)) break;
+        tc_fence_after();
+        const uint32_t a0 = stages_s + (uint32_t)(s * kStageBytes);
+        const uint32_t b0 = a0 + kABytes;
+        // the K steps (32 frames each) the piece touches
+        const int k0 = pc.lo >> 5, k1 = (pc.hi + 31) >> 5;
+        for (int k = k0; k < k1; ++k)
+          mma_f8(tmem + kIncCol, sw128_desc(a0 + 32u * k), sw128_desc(b0 + 32u * k),
+                 (first && k == k0) ? 0u : 1u);
+        issued = true;
+        first = false;
+        mma_commit(&S.empty[s]);
+        if (++s == kStages) {
+          s = 0;
+          ph ^= 1u;
+        }
+        if (pc.last) {
+          mma_commit(&S.accfull);
+          ++nsnap;
+          // wait until the epilogue has added this step's counts to the
+          // cumulative ones; the next step starts from zero
+          if (!wait_bar(S, &S.accempty, (nsnap - 1) & 1u, flag)) break;
           tc_fence_after();
-          const uint32_t a0 = smem_u32(stages + s * kStageBytes);
-          const uint32_t b0 = a0 + kABytes;
-          const int nk = (int)((f1 - f0 + 31) / 32);
-          for (int k = 0; k < nk; ++k) {
-            mma_f8(tmem + kIncCol, sw128_desc(a0 + 32u * k), sw128_desc(b0 + 32u * k),
-                   (first && k == 0) ? 0u : 1u);
-          }
-          issued = true;
-          first = false;
-          mma_commit(&S.empty[s]);
-          s = (s + 1) % kStages;
-          if (last) {
-            mma_commit(&S.accfull);
-            ++nsnap;
-            // wait until the epilogue has added this step's counts to the
-            // cumulative ones; the next step starts from zero
-            if (!wait_bar(S, &S.accempty, (nsnap - 1) & 1u, flag)) { ok = false; break; }
-            tc_fence_after();
-            first = true;
-          }
+          first = true;
         }
       }
       if (issued) {
         // drain: every MMA issued by this thread has completed
         mma_commit(&S.drain);
-        const long long t0 = clock64();
-        while (!mbar_try_wait(&S.drain, 0)) {
-          if (clock64() - t0 > kWaitCycles) {
-            atomicOr(flag, kFlagTimeout);
-            break;
-          }
-        }
+        wait_landed(&S.drain, 0, flag);
       }
     }
     __syncwarp();
-  } else if (warp <= kProducerWarps) {
-    // ---- producers: warps 1+p, 1+p+kStages, ... build every chunk c with
-    // c % kStages == p, warp rank h marking the DOF slots h, h+kPerStage, ...
-    const int p = (warp - 1) % kStages;
-    const int h = (warp - 1) / kStages;
-    const uint32_t stage_s = stages_s + (uint32_t)(p * kStageBytes);
-    uint32_t ph = 0;
-    bool used = false;
-    const uint32_t sink = smem_u32(&S.sink);
-    const int pw = warp - 1;
-    SlotInfo *sl = S.slots[pw];
-    uint32_t addr[kLaneMarks];   // one-hot positions set for the stage's occupant
-    uint32_t pb[kSlotsPerWarp];
-    ChunkWalker walk;
-    walk.start(blockIdx.x, gridDim.x, P.ntiles, P.step_size, P.nsteps);
-    ChunkPos cur;
-    for (int i = 0; i <= p; ++i) cur = walk.next();   // this warp's first chunk
-    uint64_t tile = ~0ull;       // tile whose slots are in sl[]
-    int nmine = 0;               // this warp's DOF slots in that tile
-    uint32_t edgemask = 0;       // slots whose DOF is cut by the tile's edge
-    // slot table of tile ti: lane i describes this warp's slot i
-    auto set_tile = [&](uint64_t ti) {
-      // every lane has finished reading the previous tile's slot table
-      // (mark_set, load_lane_bins) before any lane overwrites its entry: a
-      // lane still marking the last chunk of the old tile would otherwise
-      // combine the old edge mask with the new slot geometry
-      __syncwarp();
+  } else if (warp == kWarpLoad) {
+    // ---- bins loader -------------------------------------------------------
+    if (lane == 0) {
+      PieceWalker walk;
+      walk.start(blockIdx.x, gridDim.x, (uint32_t)P.ntiles, (uint32_t)P.step_size, P.nsteps);
+      int bs = 0;
+      uint32_t round = 0;        // uses of the ring so far, per slot
+      uint32_t tile = ~0u;
+      int d0a = 0, d0b = 0;
+      uint64_t n = 0;
+      for (;;) {
+        const Piece pc = walk.next();
+        if (!pc.valid) break;
+        // the producers have read this slot's previous piece
+        if (round > 0 && !wait_bar<128>(S, &S.bempty[bs], (round - 1) & 1u, flag)) break;
+        if (pc.ti != tile) {
+          StageMeta m;
+          tile_geometry(P, P.tiles[pc.ti], m);
+          d0a = m.d0a;
+          d0b = m.d0b;
+          tile = pc.ti;
+        }
+        const uint32_t dst = bins_s + (uint32_t)(bs * kBinBytes);
+        mbar_expect_tx(&S.bfull[bs], kBinBytes);
+        tma_load_2d(dst, &map_a, (int)(pc.blk * kChunk), d0a, &S.bfull[bs]);
+        tma_load_2d(dst + kMaxSlotsA * kChunk, &map_b, (int)(pc.blk * kChunk), d0b, &S.bfull[bs]);
+        ++n;
+        if (++bs == kBinStages) {
+          bs = 0;
+          ++round;
+        }
+      }
+      // every load issued has landed before the CTA may exit
+      for (int b = 0; b < kBinStages; ++b) {
+        const uint64_t uses = n > (uint64_t)b ? (n - b + kBinStages - 1) / kBinStages : 0;
+        if (uses) wait_landed(&S.bfull[b], (uint32_t)((uses - 1) & 1u), flag);
+      }
+    }
+    __syncwarp();
+  } else if (warp < kWarpEpi) {
+    // ---- producers: the team of warps 2 + p, 2 + p + kStages, ... builds
+    // the pieces n with n % kStages == p into operand stage p; its warp h
+    // rewrites row groups h, h + kPerTeam, ... (groups 0-3 the A tile, 4-11
+    // the B tile), lane (g, s) segment g of rows 32 * group + 8s .. + 7
+    const int pw = warp - kWarpProd;
+    const int team = pw % kStages;
+    const int h = pw / kStages;
+    const int g = lane & 7;
+    const uint32_t g16 = (uint32_t)g << 4;
+    const int sub8 = 8 * (lane >> 3);
+    const int nb = P.nb;
+    const uint32_t nomask[4] = {~0u, ~0u, ~0u, ~0u};
+    // per row group k of this warp, the lane's rows in the current tile:
+    // the first is bin bin0 of the DOF whose bins row lies at lds0 in a ring
+    // slot; from row `split` on, the next DOF's (at lds1)
+    int bin0[kGroupsPerWarp], split[kGroupsPerWarp];
+    uint32_t lds0[kGroupsPerWarp], lds1[kGroupsPerWarp];
+    auto geometry = [&](uint32_t ti) {
       StageMeta m;
       tile_geometry(P, P.tiles[ti], m);
-      const int slot = h + lane * kPerStage;
-      const bool valid = lane < kSlotsPerWarp && slot < m.nda + m.ndb;
-      bool edge = false;
-      if (valid) {
-        bool isA;
-        int dof, base;
-        slot_info(P, m, slot, isA, dof, base);
-        const int rows = isA ? kTileM : kTileN;
-        SlotInfo si;
-        si.src = ((uint64_t)dof * P.nschemes + P.scheme) * P.nframes;
-        si.tb = stage_s + (isA ? 0u : (uint32_t)kABytes) + ((uint32_t)base << 7);
-        si.base = base;
-        si.rows = rows;
-        si.pad = 0;
-        sl[lane] = si;
-        edge = base < 0 || base + P.nb > rows;
+#pragma unroll
+      for (int k = 0; k < kGroupsPerWarp; ++k) {
+        const int rg = h + kPerTeam * k;
+        const bool isA = rg < kGroupsA;
+        const int r0 = (isA ? m.rb + 32 * rg : m.cb + 32 * (rg - kGroupsA)) + sub8;
+        const int dof0 = r0 / nb;
+        bin0[k] = r0 - dof0 * nb;
+        split[k] = nb - bin0[k];
+        // staged DOF rows: the A tile's from row 0, the B tile's from row
+        // kMaxSlotsA; rows past the matrix read the zero fill
+        const int first = isA ? 0 : kMaxSlotsA;
+        const int lastrow = isA ? kMaxSlotsA - 1 : kBinRows - 1;
+        const int slot = min(first + dof0 - (isA ? m.d0a : m.d0b), lastrow);
+        lds0[k] = (uint32_t)slot * kChunk + g16;
+        lds1[k] = (uint32_t)min(slot + 1, lastrow) * kChunk + g16;
       }
-      nmine = __popc(__ballot_sync(0xffffffffu, valid));
-      edgemask = __ballot_sync(0xffffffffu, edge);
-      tile = ti;
-      __syncwarp();
     };
-    int nvalid = 0;
-    if (cur.valid) {
-      set_tile(cur.ti);
-      nvalid = (int)(cur.f1 - cur.f0);
-      load_lane_bins(P, sl, nmine, nvalid, cur.f0, lane, pb);
-    }
-    // Fetch this warp's next chunk (kStages on); true when it lies in the
-    // same tile as the chunk just marked.
-    auto fetch = [&]() -> bool {
-      for (int i = 0; i < kStages; ++i) cur = walk.next();
-      if (!cur.valid) return false;
-      const bool same = cur.ti == tile;
-      if (!same) set_tile(cur.ti);
-      nvalid = (int)(cur.f1 - cur.f0);
-      load_lane_bins(P, sl, nmine, nvalid, cur.f0, lane, pb);
-      return same;
-    };
-    uint32_t cph = 0;            // phase of S.cleared[p]
-    bool aborted = false;
-    // Outer loop: one pass per tile.  Its first chunk is marked here; when
-    // the stage comes from another tile, the other warps of this stage own
-    // rows this warp may have marked (and the reverse), so every warp of the
-    // stage clears its previous chunk before any sets the new one.  All
-    // warps of a stage walk the same chunks, so they all meet here.  The
-    // tile's other chunks are marked by the inner loop, which holds no
-    // barrier code (with it, the marking loop compiles to slower code).
-    while (cur.valid && !aborted) {
+    // bounded wait by lane 0, then every lane acquires the completed phase
+    auto warp_wait = [&](uint64_t *bar, uint32_t parity) -> bool {
       int go = 1;
-      if (lane == 0 && used) go = wait_bar(S, &S.empty[p], ph, flag) ? 1 : 0;
+      if (lane == 0) go = wait_bar(S, bar, parity, flag) ? 1 : 0;
       go = __shfl_sync(0xffffffffu, go, 0);
-      if (!go) break;
-      if (used) {
-        ph ^= 1u;
-        mark_clear(addr);
-        __syncwarp();
-        int ok = 1;
-        if (lane == 0) {
-          mbar_arrive(&S.cleared[p]);
-          ok = wait_bar(S, &S.cleared[p], cph, flag) ? 1 : 0;
-        }
-        cph ^= 1u;
-        ok = __shfl_sync(0xffffffffu, ok, 0);
-        if (!ok) break;
+      if (go) mbar_try_wait(bar, parity);
+      return go != 0;
+    };
+    PieceWalker walk;
+    walk.start(blockIdx.x, gridDim.x, (uint32_t)P.ntiles, (uint32_t)P.step_size, P.nsteps);
+    Piece pc;
+    for (int i = 0; i <= team; ++i) pc = walk.next();
+    uint32_t n = (uint32_t)team;   // index of the piece among the CTA's pieces
+    uint32_t tile = ~0u;
+    uint32_t use = 0;              // earlier pieces built into this stage
+    uint8_t *const stage = stages + team * kStageBytes;
+    while (pc.valid) {
+      if (pc.ti != tile) {
+        geometry(pc.ti);
+        tile = pc.ti;
       }
-      __syncwarp();
-      mark_set(P, sl, nmine, edgemask, nvalid, sink, lane, pb, addr, flag);
+      const int bs = (int)(n & (kBinStages - 1));
+      if (!warp_wait(&S.bfull[bs], (n / kBinStages) & 1u)) break;
+      // the MMA has consumed this stage's previous piece
+      if (use > 0 && !warp_wait(&S.empty[team], (use - 1) & 1u)) break;
+      const uint32_t src = bins_s + (uint32_t)(bs * kBinBytes);
+      uint4 wc[kGroupsPerWarp], wn[kGroupsPerWarp];
+#pragma unroll
+      for (int k = 0; k < kGroupsPerWarp; ++k) {
+        wc[k] = lds128(src + lds0[k]);
+        wn[k] = kSplit ? lds128(src + lds1[k]) : wc[k];
+      }
+      const bool partial = pc.lo > 0 || pc.hi < kChunk;
+      uint32_t fm[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) fm[j] = frame_mask(pc.lo - 16 * g - 4 * j, pc.hi - 16 * g - 4 * j);
+#pragma unroll
+      for (int k = 0; k < kGroupsPerWarp; ++k) {
+        const int rg = h + kPerTeam * k;
+        const bool isA = rg < kGroupsA;
+        uint8_t *group = stage + (isA ? 32 * rg * kChunk : kABytes + 32 * (rg - kGroupsA) * kChunk) +
+                         sub8 * kChunk;
+        if (isA && partial)   // frames of the block outside the piece read zero in A
+          build_rows<kMode, kSplit, true>(group, g16, wc[k], wn[k], bin0[k], split[k], nb, fm);
+        else
+          build_rows<kMode, kSplit, false>(group, g16, wc[k], wn[k], bin0[k], split[k], nb, nomask);
+      }
+      // the ring slot is released once its values have been used: an
+      // arrive right after the loads did not keep them ahead of the
+      // loader's next copy into the slot
+      mbar_arrive(&S.bempty[bs]);
       fence_proxy_async();
-      mbar_arrive(&S.full[p]);
-      used = true;
-      bool more = fetch();
-      while (more) {
-        // wait until the MMA has consumed this stage's previous chunk
-        go = 1;
-        if (lane == 0) go = wait_bar(S, &S.empty[p], ph, flag) ? 1 : 0;
-        go = __shfl_sync(0xffffffffu, go, 0);
-        if (!go) {
-          aborted = true;
-          break;
-        }
-        ph ^= 1u;
-        mark_clear(addr);
-        __syncwarp();
-        mark_set(P, sl, nmine, edgemask, nvalid, sink, lane, pb, addr, flag);
-        fence_proxy_async();
-        mbar_arrive(&S.full[p]);
-        more = fetch();
-      }
+      mbar_arrive(&S.full[team]);
+      ++use;
+      for (int i = 0; i < kStages; ++i) pc = walk.next();
+      n += kStages;
     }
   } else {
     // ---- epilogue ------------------------------------------------------------
     const int ew = warp & 3;             // TMEM lane group of this warp
     const int etid = 32 * ew + lane;     // accumulator row
-    const int eth = 32 * (warp - 1 - kProducerWarps) + lane;   // 0 .. kEpilogue-1
+    const int eth = 32 * (warp - kWarpEpi) + lane;   // 0 .. kEpilogue-1
     const int col0 = (eth / 128) * kEpiCols;                  // this quartet's columns
     uint32_t nsnap = 0;
     bool ok = true;
@@ -695,7 +684,7 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__
       const int seg_max = min(32, nb);       // longest segment (warp-uniform)
       for (int t = 0; t < P.nsteps; ++t) {
         if (eth == 0) {
-          bool go = wait_bar(S, &S.accfull, nsnap & 1u, flag);
+          bool go = wait_bar<256>(S, &S.accfull, nsnap & 1u, flag);
           if (*(volatile int *)&S.abort_flag) go = false;
           S.ego[nsnap & 1u] = go ? 1 : 0;
         }
@@ -764,14 +753,15 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__
           uint32_t v[kEpiW];
           tmem_ld_w(trow + (uint32_t)(chunk * kEpiW), v);
           tmem_wait_ld_w(v);
-          // exact integer counts from the FP32 accumulator; F(c) from the
-          // shared table, larger counts from the global table
+          // exact integer counts from the FP32 accumulator (4 per frame);
+          // F(c) from the shared table, larger counts from the global table
           unsigned cnt[kEpiW];
           unsigned long long cv[kEpiW];
           bool big = false;
 #pragma unroll
           for (int q = 0; q < kEpiW; ++q) {
-            cnt[q] = __float_as_uint(__uint_as_float(v[q]) + 8388608.0f) - 0x4B000000u;
+            cnt[q] = __float_as_uint(fmaf(__uint_as_float(v[q]), 0.25f, 8388608.0f)) -
+                     0x4B000000u;
             big |= cnt[q] >= (unsigned)kTabTc;
             cv[q] = S.tab[min(cnt[q], (unsigned)kTabTc - 1u)];
           }
@@ -836,7 +826,7 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__
   // ---- tear-down -----------------------------------------------------------
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (warp == kWarpMma) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(kTmemCols)
@@ -844,14 +834,76 @@ pairs_tc_kernel(const __grid_constant__ TcParams P, const unsigned long long *__
   }
 }
 
-size_t tc_smem_bytes() { return 1024 + (size_t)kStages * kStageBytes + sizeof(Smem); }
+// Checks every bin of the scheme against nb (a bin outside [0, nb) sets
+// kFlagBinRange) and, when dst is set, copies the scheme's rows to dst with
+// a row pitch of `pitch` bytes (a multiple of 16, as TMA needs).  Thread x of
+// block row y handles 16 frames of DOF y, y + gridDim.y, ...
+__global__ void tc_bins_kernel(const uint8_t *__restrict__ bins, uint64_t nframes, int nschemes,
+                               int scheme, uint32_t ndof, int nb, uint8_t *__restrict__ dst,
+                               uint64_t pitch, int *__restrict__ flag) {
+  const uint64_t f0 = 16ull * (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x);
+  if (f0 >= nframes) return;
+  const int nv = (int)(nframes - f0 < 16 ? nframes - f0 : 16);
+  const uint32_t lim = 0x01010101u * (uint32_t)nb;
+  bool bad = false;
+  for (uint32_t d = blockIdx.y; d < ndof; d += gridDim.y) {
+    const uint8_t *src = bins + ((uint64_t)d * nschemes + scheme) * nframes + f0;
+    uint32_t w[4];
+    if (nv == 16 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+      const uint4 v = __ldg(reinterpret_cast<const uint4 *>(src));
+      w[0] = v.x;
+      w[1] = v.y;
+      w[2] = v.z;
+      w[3] = v.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        uint32_t x = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (4 * j + q < nv) x |= (uint32_t)__ldg(src + 4 * j + q) << (8 * q);
+        w[j] = x;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) bad |= __vcmpgeu4(w[j], lim) != 0u;
+    if (dst)
+      *reinterpret_cast<uint4 *>(dst + (uint64_t)d * pitch + f0) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  if (bad) atomicOr(flag, kFlagBinRange);
+}
+
+size_t tc_smem_bytes() {
+  return 1024 + (size_t)kStages * kStageBytes + (size_t)kBinStages * kBinBytes + sizeof(Smem);
+}
+static_assert(1024 + kStages * kStageBytes + kBinStages * kBinBytes + sizeof(Smem) <= 232448,
+              "shared memory of the tensor-core count kernel above 227 KB");
+static_assert(kThreads == 704 && kRowGroups == kPerTeam * kGroupsPerWarp, "warp roles");
+static_assert((kBinStages & (kBinStages - 1)) == 0 && kBinStages % kStages == 0, "bins ring");
+
+template <int kMode, bool kSplit>
+int launch_tc(centre_ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, const TcParams &P,
+              unsigned grid, const unsigned long long *d_fix, unsigned long long *d_sclnc,
+              unsigned *d_nnz) {
+  auto kern = pairs_tc_kernel<kMode, kSplit>;
+  const size_t smem = tc_smem_bytes();
+  CENTRE_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+  {
+    KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
+    kern<<<grid, kThreads, smem, ctx->stream>>>(ma, mb, P, d_fix, d_sclnc, d_nnz, ctx->d_flag);
+  }
+  ctx->launches++;
+  CENTRE_CUDA(ctx, cudaGetLastError());
+  return CENTRE_OK;
+}
 
 }  // namespace
 
 bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes) {
   if (ctx->cc_major != 10 || ctx->cc_minor != 3) return false;  // sm_103a build
   if (nb < kMinBins || nb > 255) return false;
-  if (nframes >= (1ull << 24)) return false;  // FP32 accumulation stays exact
+  if (nframes > (1ull << 22)) return false;  // FP32 sums of 4 per frame stay exact
   return true;
 }
 
@@ -859,6 +911,7 @@ int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const unsigned long l
                     unsigned long long *d_sclnc, unsigned *d_nnz) {
   const int nb = PP.nb;
   const uint32_t ndof = PP.ndof;
+  const uint64_t nframes = PP.nframes;
   const uint64_t nrows = (uint64_t)ndof * nb;
   if (nrows >= (1ull << 31)) return set_error(ctx, CENTRE_E_UNSUPPORTED, "too many DOF bins");
   // tiles (row tile, column tile) holding at least one pair i < j
@@ -874,9 +927,50 @@ int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const unsigned long l
     }
   }
   if (tiles.empty()) return CENTRE_OK;
+  if (tiles.size() >= (1ull << 32)) return set_error(ctx, CENTRE_E_UNSUPPORTED, "too many tiles");
+  auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tensor_map_encoder());
+  if (!encode) return set_error(ctx, CENTRE_E_CUDA, "cuTensorMapEncodeTiled unavailable");
   int st = CENTRE_OK;
   uint2 *d_tiles = (uint2 *)scratch(ctx, kSlotPairs, sizeof(uint2) * tiles.size(), &st);
   if (!d_tiles) return st;
+  // The scheme's bins as a 2-D tensor of nframes bytes per DOF row.  TMA
+  // wants a 16-byte aligned base and row pitch: the bins array itself when
+  // nframes is a multiple of 16, else a copy with the pitch rounded up.
+  const uint8_t *base = PP.bins + (uint64_t)PP.scheme * nframes;
+  uint64_t pitch = (uint64_t)PP.nschemes * nframes;
+  uint8_t *copy = nullptr;
+  if (nframes % 16 != 0 || (reinterpret_cast<uintptr_t>(PP.bins) & 15u) != 0) {
+    pitch = (nframes + 15) / 16 * 16;
+    copy = (uint8_t *)scratch(ctx, kSlotTcBins, pitch * ndof, &st);
+    if (!copy) return st;
+    base = copy;
+  }
+  {
+    const uint64_t nthr = (nframes + 15) / 16;
+    const dim3 grid((unsigned)((nthr + 255) / 256), std::min<uint32_t>(ndof, 2048u));
+    tc_bins_kernel<<<grid, 256, 0, ctx->stream>>>(PP.bins, nframes, PP.nschemes, PP.scheme, ndof,
+                                                  nb, copy, pitch, ctx->d_flag);
+    ctx->launches++;
+    CENTRE_CUDA(ctx, cudaGetLastError());
+  }
+  CUtensorMap ma, mb;
+  {
+    const cuuint64_t gdim[2] = {nframes, ndof};
+    const cuuint64_t gstride[1] = {pitch};
+    const cuuint32_t box_a[2] = {(cuuint32_t)kChunk, (cuuint32_t)kMaxSlotsA};
+    const cuuint32_t box_b[2] = {(cuuint32_t)kChunk, (cuuint32_t)kMaxSlotsB};
+    const cuuint32_t estride[2] = {1, 1};
+    CUresult cr = encode(&ma, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t *>(base), gdim,
+                         gstride, box_a, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr == CUDA_SUCCESS)
+      cr = encode(&mb, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t *>(base), gdim,
+                  gstride, box_b, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) return set_error(ctx, CENTRE_E_CUDA, "cuTensorMapEncodeTiled failed");
+  }
   CENTRE_CUDA(ctx, cudaMemcpyAsync(d_tiles, tiles.data(), sizeof(uint2) * tiles.size(),
                                    cudaMemcpyHostToDevice, ctx->stream));
   const uint64_t npairs = (uint64_t)ndof * (ndof - 1) / 2;
@@ -884,29 +978,24 @@ int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const unsigned long l
                                    ctx->stream));
   CENTRE_CUDA(ctx, cudaMemsetAsync(d_nnz, 0, sizeof(unsigned) * npairs * PP.nsteps, ctx->stream));
   TcParams P;
-  P.bins = PP.bins;
   P.tiles = d_tiles;
   P.ntiles = tiles.size();
-  P.nframes = PP.nframes;
   P.step_size = PP.step_size;
   P.ndof = ndof;
   P.nrows = (uint32_t)nrows;
-  P.nschemes = PP.nschemes;
-  P.scheme = PP.scheme;
   P.nb = nb;
   P.nsteps = PP.nsteps;
   P.fix_scale = PP.fix_scale;
-  const size_t smem = tc_smem_bytes();
-  CENTRE_CUDA(ctx, cudaFuncSetAttribute(pairs_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
   const unsigned grid = (unsigned)std::min<uint64_t>(tiles.size(), (uint64_t)ctx->sm_count);
-  {
-    KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
-    pairs_tc_kernel<<<grid, kThreads, smem, ctx->stream>>>(P, d_fix, d_sclnc, d_nnz, ctx->d_flag);
-  }
-  ctx->launches++;
-  CENTRE_CUDA(ctx, cudaGetLastError());
-  return CENTRE_OK;
+  const bool split = nb % 8 != 0;   // a lane's 8 rows may span two DOFs
+  if (nb <= 64)
+    return split ? launch_tc<0, true>(ctx, ma, mb, P, grid, d_fix, d_sclnc, d_nnz)
+                 : launch_tc<0, false>(ctx, ma, mb, P, grid, d_fix, d_sclnc, d_nnz);
+  if (nb <= 128)
+    return split ? launch_tc<1, true>(ctx, ma, mb, P, grid, d_fix, d_sclnc, d_nnz)
+                 : launch_tc<1, false>(ctx, ma, mb, P, grid, d_fix, d_sclnc, d_nnz);
+  return split ? launch_tc<2, true>(ctx, ma, mb, P, grid, d_fix, d_sclnc, d_nnz)
+               : launch_tc<2, false>(ctx, ma, mb, P, grid, d_fix, d_sclnc, d_nnz);
 }
 
 }  // namespace centre

@@ -58,7 +58,8 @@ enum { CENTRE_ML = 0, CENTRE_MM = 1, CENTRE_CS = 2, CENTRE_JS = 3 };
 enum {
   CENTRE_COUNTS_AUTO = 0,   /* histogram form where it fits, else TC      */
   CENTRE_COUNTS_ATOMIC = 1, /* shared-memory atomic histograms            */
-  CENTRE_COUNTS_TC = 2      /* FP8 one-hot O^T O on tcgen05 tensor cores  */
+  CENTRE_COUNTS_TC = 2      /* FP8 one-hot O^T O on tcgen05 tensor cores
+                             * (16-255 bins, at most 2^22 frames)        */
 };
 
 /* Entropy-stage parameters ([entropy]/[control]/[histogram] keys of the

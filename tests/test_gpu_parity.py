@@ -388,8 +388,15 @@ def oracle_moments(orc, bins, nsteps, nb):
 
 @pytest.mark.parametrize("natoms,nframes,nsteps,nb", [
     (4, 4_096, 1, 50), (8, 20_000, 4, 50), (12, 10_007, 3, 30), (30, 30_000, 10, 16),
-    (10, 12_000, 2, 100), (6, 8_000, 2, 255)])
+    (10, 12_000, 2, 100), (6, 8_000, 2, 255), (9, 6_000, 3, 32), (7, 5_001, 2, 64),
+    (6, 4_000, 2, 128), (5, 3_000, 2, 136), (7, 1_000, 10, 24), (6, 997, 7, 17)])
 def test_tc_counts_identical_to_atomic(gpu, orc, natoms, nframes, nsteps, nb):
+    """Moments of the tensor-core form against the oracle's counts and the
+    histogram form.  The cases cover the three one-hot encodings (bins below
+    64, below 128, up to 255), bin counts whose 8-row groups stay inside one
+    DOF (multiples of 8) and ones that straddle two, frame counts that are not
+    multiples of 16 (the bins are re-pitched for TMA), and convergence steps
+    shorter than a 128-frame block (several step ends inside one block)."""
     tr = chain_trajectory(natoms, nframes, seed=natoms * 7 + nb)
     bins, ext, types = stack_blocks(tr, gpu, [nb])
     pa = make_params(nframes, nsteps, [nb], [0, 1], True, counts_form=1)
@@ -407,6 +414,31 @@ def test_tc_counts_identical_to_atomic(gpu, orc, natoms, nframes, nsteps, nb):
         s_at = gpu.entropy2d(pa, types, bins, ext)
         s_tc = gpu.entropy2d(pt, types, bins, ext)
         assert np.array_equal(s_at, s_tc)
+
+
+def test_tc_second_scheme(gpu):
+    """Two bin schemes: the tensor-core form reads the second scheme's rows
+    (an offset of nframes into each DOF's bins) and matches the histogram
+    form bit for bit on both."""
+    tr = chain_trajectory(9, 8_000, seed=91)
+    bins, ext, types = stack_blocks(tr, gpu, [16, 40])
+    pa = make_params(8_000, 4, [16, 40], [0, 1], True, counts_form=1)
+    pt = make_params(8_000, 4, [16, 40], [0, 1], True, counts_form=2)
+    for sch in (0, 1):
+        ca, za, sa = gpu.pair_moments(pa, bins, scheme=sch)
+        ct, zt, st = gpu.pair_moments(pt, bins, scheme=sch)
+        assert sa == st and np.array_equal(ca, ct) and np.array_equal(za, zt)
+    assert np.array_equal(gpu.entropy2d(pa, types, bins, ext), gpu.entropy2d(pt, types, bins, ext))
+
+
+def test_tc_rejects_bins_out_of_range(gpu):
+    from centre_gb300.api import CentreError
+    tr = chain_trajectory(5, 4_000, seed=3)
+    bins, ext, types = stack_blocks(tr, gpu, [20])
+    bins[2, 0, 1234] = 20
+    pt = make_params(4_000, 2, [20], [0], True, counts_form=2)
+    with pytest.raises(CentreError):
+        gpu.pair_moments(pt, bins)
 
 
 @pytest.mark.parametrize("natoms,nframes,nsteps,nb", [
