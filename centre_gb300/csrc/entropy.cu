@@ -77,9 +77,10 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
   const uint64_t per = (uint64_t)P.nests * P.nschemes * P.nsteps;
 
   const int warp = tid >> 5, nwarps = blockDim.x >> 5;
-  // 32-bit loads need every row start 4-byte aligned: the frame count and
-  // the caller's bins pointer (an offset view may not be)
-  const bool word = ((n & 3) == 0) && ((reinterpret_cast<uintptr_t>(bins) & 3) == 0);
+  // four frames per 32-bit load; a row that does not start on a 4-byte
+  // boundary takes each word from the two aligned words around it
+  const uint32_t rsh = 8u * (uint32_t)(reinterpret_cast<uintptr_t>(row) & 3u);
+  const uint32_t *rw = reinterpret_cast<const uint32_t *>(row - (rsh >> 3));
   const uint32_t lim = 0x01010101u * (uint32_t)nb;
   for (int t = 0; t < P.nsteps; ++t) {
     for (int b = tid; b < 8 * 256; b += blockDim.x) whist[b] = 0;
@@ -92,13 +93,12 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
       if (v >= (unsigned)nb) bad = 1;
       else atomicAdd(&wh[v], 1u);
     };
-    if (word) {
+    {
       const uint64_t g0 = (f0 + 3) >> 2, g1 = f1 >> 2;
       for (uint64_t f = f0 + tid; f < min(f1, g0 << 2); f += blockDim.x) one(f);
       for (uint64_t f = max(f0, g1 << 2) + tid; f < f1; f += blockDim.x) one(f);
-      const uint32_t *rw = reinterpret_cast<const uint32_t *>(row);
       for (uint64_t g = g0 + tid; g < g1; g += blockDim.x) {
-        const uint32_t w = __ldg(rw + g);
+        const uint32_t w = rsh ? __funnelshift_r(__ldg(rw + g), __ldg(rw + g + 1), rsh) : __ldg(rw + g);
         if (__vcmpgeu4(w, lim)) {
           bad = 1;
           continue;
@@ -108,8 +108,6 @@ entropy1d_kernel(const uint8_t *__restrict__ bins, const uint8_t *__restrict__ t
         atomicAdd(&wh[(w >> 16) & 255u], 1u);
         atomicAdd(&wh[w >> 24], 1u);
       }
-    } else {
-      for (uint64_t f = f0 + tid; f < f1; f += blockDim.x) one(f);
     }
     if (bad) badrange = 1;
     __syncthreads();
@@ -346,7 +344,8 @@ __device__ void decode_all_pairs_tile(uint64_t id, uint64_t ntile, uint64_t stri
 // current group's increments (kHistPrefetch).
 // `tabf` holds F(c) (the fixed-point c ln c of clnc_fix) for c < kTabF in
 // shared memory, `gfix` for c < 2^16 in global memory.
-template <int R, int C, bool kCounts, bool kBatchedRed, bool kIlv = false, bool kNnz = true>
+template <int R, int C, bool kCounts, bool kBatchedRed, bool kIlv = false, bool kNnz = true,
+          bool kAlign = true>
 __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_t *cols_s,
                          const uint64_t *out_s, unsigned *hist,
                          const unsigned long long *tabf,
@@ -366,9 +365,14 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
   const uint32_t cstride = kIlv ? 4u * NP : 4u;
   const uint8_t *bins = J.bins;
   const uint32_t hist_s = (uint32_t)__cvta_generic_to_shared(hist);
-  // DOF rows as 32-bit word offsets (row starts are 4-byte aligned when the
-  // word path is used; the byte path rebuilds the byte offset)
-  const uint32_t *bw = reinterpret_cast<const uint32_t *>(bins);
+  // DOF rows as 32-bit word offsets from the aligned word at or before the
+  // bins pointer.  kAlign (frame count and bins pointer multiples of 4):
+  // every row starts on a word.  Otherwise a row that does not start on a
+  // 4-byte boundary is read four frames at a time from the two aligned words
+  // around them (a funnel shift); the second word holds the group's last
+  // byte, so no load leaves the word of a valid byte.
+  const uint32_t mis = kAlign ? 0u : (uint32_t)(reinterpret_cast<uintptr_t>(bins) & 3u);
+  const uint32_t *bw = reinterpret_cast<const uint32_t *>(bins - mis);
   const uint32_t nb4 = 4u * (uint32_t)nb;
   // Bin range check four bytes at a time.  Up to 128 bins a byte x is out
   // of range (x >= nb) exactly when bit 7 of x | (x + 128 - nb) is set: below
@@ -379,26 +383,28 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
   const bool small_nb = nb <= 128;
   const uint32_t range_add = small_nb ? 0x01010101u * (uint32_t)(128 - nb) : 0u;
   const uint32_t lim = 0x01010101u * (uint32_t)nb;
-  // 32-bit loads need every row start 4-byte aligned: the frame count and
-  // the caller's bins pointer (an offset view may not be)
-  const bool word = ((n & 3) == 0) && ((reinterpret_cast<uintptr_t>(bins) & 3) == 0);
   int bad = 0;
 
   // row/column word offsets and histogram addresses; with the batched
   // reduction they are recomputed every step so that none of them is live
   // across the reduction, which then has the registers to itself
   uint32_t rw0[R], cw0[C];
+  uint32_t rsh[R], csh[C];   // bit shift of each row start within its word
   uint32_t rconst[R], cconst[C];
   auto setup = [&]() {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      rw0[r] = (uint32_t)((((uint64_t)rows_s[r] * J.nschemes + J.scheme) * n) >> 2);
+      const uint64_t o = mis + ((uint64_t)rows_s[r] * J.nschemes + J.scheme) * n;
+      rw0[r] = (uint32_t)(o >> 2);
+      rsh[r] = 8u * (uint32_t)(o & 3u);
       rconst[r] = kIlv ? hist_s + 4u * (uint32_t)(((r + rrot) % R) * C)
                        : hist_s + 4u * (uint32_t)(r * C * nb2);
     }
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-      cw0[c] = (uint32_t)((((uint64_t)cols_s[c] * J.nschemes + J.scheme) * n) >> 2);
+      const uint64_t o = mis + ((uint64_t)cols_s[c] * J.nschemes + J.scheme) * n;
+      cw0[c] = (uint32_t)(o >> 2);
+      csh[c] = 8u * (uint32_t)(o & 3u);
       cconst[c] = kIlv ? 4u * (uint32_t)((c + crot) % C) : 4u * (uint32_t)(c * nb2);
     }
   };
@@ -459,7 +465,7 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
           for (int c = 0; c < C; ++c) red_shared_inc(rconst[r] + a[r] * nb4 + cconst[c] + 4u * b[c]);
       }
     };
-    if (word) {
+    {
       const uint64_t g0 = (f0 + 3) >> 2, g1 = f1 >> 2;   // whole 4-frame groups
       for (uint64_t f = f0 + tid; f < min(f1, g0 << 2); f += blockDim.x) one_frame(f);
       for (uint64_t f = max(f0, g1 << 2) + tid; f < f1; f += blockDim.x) one_frame(f);
@@ -467,9 +473,15 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
       // increments (the red.shared asm keeps later loads behind it)
       auto load_group = [&](uint64_t g, uint32_t (&x)[R], uint32_t (&y)[C]) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) x[r] = __ldg(bw + rw0[r] + (uint32_t)g);
+        for (int r = 0; r < R; ++r) {
+          const uint32_t *w = bw + rw0[r] + (uint32_t)g;
+          x[r] = (!kAlign && rsh[r]) ? __funnelshift_r(__ldg(w), __ldg(w + 1), rsh[r]) : __ldg(w);
+        }
 #pragma unroll
-        for (int c = 0; c < C; ++c) y[c] = __ldg(bw + cw0[c] + (uint32_t)g);
+        for (int c = 0; c < C; ++c) {
+          const uint32_t *w = bw + cw0[c] + (uint32_t)g;
+          y[c] = (!kAlign && csh[c]) ? __funnelshift_r(__ldg(w), __ldg(w + 1), csh[c]) : __ldg(w);
+        }
       };
       // one 4-frame group: range check, rotation, 4 x R x C increments
       auto count_group = [&](uint32_t (&rw)[R], uint32_t (&cw)[C]) {
@@ -530,8 +542,6 @@ __device__ int hist_tile(const HistJob &J, const uint32_t *rows_s, const uint32_
           count_group(rw, cw);
         }
       }
-    } else {
-      for (uint64_t f = f0 + tid; f < f1; f += blockDim.x) one_frame(f);
     }
     __syncthreads();
     if (kCounts) {
@@ -725,9 +735,13 @@ pairs_hist_kernel(const uint8_t *__restrict__ bins, const PairTask *__restrict__
   J.sclnc = sclnc;
   J.nnz = nnz;
   J.counts = counts;
-  const int bad = hist_tile<R, C, kCounts, true, kHistInterleave && R == 4 && C == 4, kNnz>(
-      J, rows_s, cols_s, out_s, hist, tabf, gfix);
-  if (bad && tid == 0) atomicOr(flag, kFlagBinRange);
+  constexpr bool kIlv = kHistInterleave && R == 4 && C == 4;
+  // rows on word boundaries take the plain 32-bit loads
+  const bool aligned = ((P.nframes & 3) == 0) && ((reinterpret_cast<uintptr_t>(bins) & 3) == 0);
+  const int bad =
+      aligned ? hist_tile<R, C, kCounts, true, kIlv, kNnz, true>(J, rows_s, cols_s, out_s, hist, tabf, gfix)
+              : hist_tile<R, C, kCounts, true, kIlv, kNnz, false>(J, rows_s, cols_s, out_s, hist, tabf, gfix);
+  if (bad) atomicOr(flag, kFlagBinRange);   // any thread may have seen it
 }
 
 // Persistent all-pairs histogram counts over several trajectories: the work
@@ -778,7 +792,9 @@ pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nit
     J.sclnc = S.sclnc;
     J.nnz = S.nnz;
     J.counts = nullptr;
-    bad |= hist_tile<R, R, false, false>(J, rows_s, cols_s, out_s, hist, tabf, gfix);
+    const bool aligned = ((J.nframes & 3) == 0) && ((reinterpret_cast<uintptr_t>(J.bins) & 3) == 0);
+    bad |= aligned ? hist_tile<R, R, false, false, false, true, true>(J, rows_s, cols_s, out_s, hist, tabf, gfix)
+                   : hist_tile<R, R, false, false, false, true, false>(J, rows_s, cols_s, out_s, hist, tabf, gfix);
   }
   if (bad) atomicOr(flag, kFlagBinRange);
 }

@@ -230,6 +230,38 @@ def test_entropy2d_rejects_bad_bins(gpu):
     assert e.value.status == -4
 
 
+def test_pair_counts_report_bad_bin_of_any_thread(gpu):
+    """A bin out of range read by any thread of the count kernel (here the
+    one that takes frames 1000-1003, not thread 0) fails the call."""
+    rng = np.random.default_rng(5)
+    bins = rng.integers(0, 30, (6, 1, 4000), dtype=np.uint8)
+    bins[4, 0, 1001] = 30
+    p = make_params(4000, 2, [30], [0, 1], True, counts_form=1)
+    with pytest.raises(CentreError) as e:
+        gpu.pair_moments(p, bins)
+    assert e.value.status == -4
+
+
+@pytest.mark.parametrize("nframes,nsteps", [(100_000, 16), (100_000, 1), (70_001, 25)])
+def test_pair_counts_of_concentrated_cells(gpu, orc, nframes, nsteps):
+    """Histogram-form moments on cells far past the shared c ln c table and
+    past 2^16 counts (three DOFs nearly constant, one exactly constant), with
+    one step of 100,000 frames and with many short steps, on a frame count
+    that is not a multiple of 4 (the byte path): equal to the oracle's."""
+    rng = np.random.default_rng(nframes + nsteps)
+    nb = 50
+    bins = rng.integers(0, nb, (7, 1, nframes), dtype=np.uint8)
+    bins[0, 0] = 7
+    for d, keep in ((1, 0.9), (2, 0.97), (3, 0.6)):
+        bins[d, 0, rng.random(nframes) < keep] = 11 + d
+    p = make_params(nframes, nsteps, [nb], [0, 1], True, counts_form=1)
+    ca, za, sa = gpu.pair_moments(p, bins)
+    xo, zo = oracle_moments(orc, bins[:, 0], nsteps, nb)
+    assert np.array_equal(za, zo)
+    np.testing.assert_allclose(ca.astype(np.float64) * 2.0 ** -sa, xo, rtol=1e-12,
+                               atol=nb * nb * 2.0 ** -(sa + 1))
+
+
 # --------------------------------------------------------------- score ----
 def reference_edge_order(types):
     """Pairs in the reference's edge-list order: B/B, B/A, B/D, A/A, A/D, D/D
