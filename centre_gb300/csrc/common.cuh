@@ -111,9 +111,11 @@ inline int flag_status(int f) {
 }
 
 // The shared-memory histogram kernels address bin rows with 32-bit word
-// offsets: a bin matrix (DOFs x schemes x frames bytes) must stay below
-// 16 GiB for them.
-constexpr uint64_t kMaxHistBinBytes = 1ull << 34;
+// offsets from the aligned word at or before the bins pointer (up to 3 bytes
+// before it, and a row's last word may be followed by one more for an
+// unaligned row): a bin matrix (DOFs x schemes x frames bytes) must stay
+// 16 bytes below 16 GiB for them.
+constexpr uint64_t kMaxHistBinBytes = (1ull << 34) - 16;
 
 // Order-preserving map of a double onto uint64 (larger double -> larger key).
 __host__ __device__ inline uint64_t order_key(double v) {
