@@ -792,9 +792,12 @@ pairs_hist_batch_kernel(const BatchSys *__restrict__ sys, int nsys, uint64_t nit
     J.sclnc = S.sclnc;
     J.nnz = S.nnz;
     J.counts = nullptr;
+    // 4 x 4 tiles: interleaved histograms and the batched quad-sweep
+    // reduction, as in the single-trajectory kernel
+    constexpr bool kIlvB = kHistInterleave && R == 4;
     const bool aligned = ((J.nframes & 3) == 0) && ((reinterpret_cast<uintptr_t>(J.bins) & 3) == 0);
-    bad |= aligned ? hist_tile<R, R, false, false, false, true, true>(J, rows_s, cols_s, out_s, hist, tabf, gfix)
-                   : hist_tile<R, R, false, false, false, true, false>(J, rows_s, cols_s, out_s, hist, tabf, gfix);
+    bad |= aligned ? hist_tile<R, R, false, kIlvB, kIlvB, true, true>(J, rows_s, cols_s, out_s, hist, tabf, gfix)
+                   : hist_tile<R, R, false, kIlvB, kIlvB, true, false>(J, rows_s, cols_s, out_s, hist, tabf, gfix);
   }
   if (bad) atomicOr(flag, kFlagBinRange);
 }
