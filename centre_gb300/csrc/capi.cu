@@ -447,6 +447,10 @@ void centre_gpu_destroy(centre_ctx *ctx) {
     cudaEventDestroy(t.b);
   }
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
+  if (ctx->copy_in) cudaStreamSynchronize(ctx->copy_in), cudaStreamDestroy(ctx->copy_in);
+  if (ctx->copy_out) cudaStreamSynchronize(ctx->copy_out), cudaStreamDestroy(ctx->copy_out);
+  for (auto e : ctx->copy_ev)
+    if (e) cudaEventDestroy(e);
   centre::batch_state_free(ctx);
   centre::screen_state_free(ctx);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -502,6 +506,21 @@ int centre_gpu_discretize_dev(centre_ctx *ctx, int bat_type, const float *data, 
                            optimize_dih, bins, extremes);
 }
 
+// DOFs per chunk below which the discretiser's transfers are not split
+static constexpr uint32_t kDiscChunkMinDofs = 64;
+
+// The context's copy-in / copy-out streams and events, created on first use
+// (not under stream capture: host-pointer entry points are never captured).
+static int copy_streams(centre_ctx *ctx) {
+  if (!ctx->copy_in)
+    CENTRE_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+  if (!ctx->copy_out)
+    CENTRE_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+  for (auto &e : ctx->copy_ev)
+    if (!e) CENTRE_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return CENTRE_OK;
+}
+
 int centre_gpu_discretize(centre_ctx *ctx, int bat_type, const float *data, uint32_t ndof,
                           uint64_t nframes, const uint8_t *bin_schemes, uint32_t nschemes,
                           uint8_t bins_ref, int optimize_dih, uint8_t *bins, double *extremes) {
@@ -517,14 +536,38 @@ int centre_gpu_discretize(centre_ctx *ctx, int bat_type, const float *data, uint
   unsigned char *d_out = (unsigned char *)scratch(ctx, kSlotBins, nbins + 32 * (size_t)ndof + 256, &st);
   if (!d_out) return st;
   double *d_ext = reinterpret_cast<double *>(d_out + ((nbins + 255) & ~size_t(255)));
-  CENTRE_CUDA(ctx, cudaMemcpyAsync(d_in, data, nin, cudaMemcpyHostToDevice, ctx->stream));
-  CENTRE_TRY(launch_discretize(ctx, bat_type, (const float *)d_in, ndof, nframes, bin_schemes,
-                               nschemes, bins_ref, optimize_dih, d_out, d_ext));
+  // DOFs are binned independently: chunks of them stream in, are binned and
+  // stream out on three streams, so the transfers overlap the kernels (and
+  // each other) instead of running before and after them
+  CENTRE_TRY(copy_streams(ctx));
+  // one flag for all chunks: the chunk launches do not reset it
+  CENTRE_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+  // the first upload waits for work already queued on the context's stream
+  // (it may still read the scratch the upload fills)
+  CENTRE_CUDA(ctx, cudaEventRecord(ctx->copy_ev[15], ctx->stream));
+  CENTRE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_in, ctx->copy_ev[15], 0));
+  const uint32_t nchunk = ndof >= 4 * kDiscChunkMinDofs ? 4u : 1u;
+  for (uint32_t c = 0; c < nchunk; ++c) {
+    const uint32_t d0 = (uint32_t)((uint64_t)ndof * c / nchunk);
+    const uint32_t d1 = (uint32_t)((uint64_t)ndof * (c + 1) / nchunk);
+    const size_t fin = (size_t)nframes * 4, fout = (size_t)nschemes * nframes;
+    cudaEvent_t in_ev = ctx->copy_ev[2 * c], done_ev = ctx->copy_ev[2 * c + 1];
+    CENTRE_CUDA(ctx, cudaMemcpyAsync(d_in + d0 * fin, data + (size_t)d0 * nframes,
+                                     (d1 - d0) * fin, cudaMemcpyHostToDevice, ctx->copy_in));
+    CENTRE_CUDA(ctx, cudaEventRecord(in_ev, ctx->copy_in));
+    CENTRE_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, in_ev, 0));
+    CENTRE_TRY(launch_discretize(ctx, bat_type, (const float *)(d_in + d0 * fin), d1 - d0, nframes,
+                                 bin_schemes, nschemes, bins_ref, optimize_dih, d_out + d0 * fout,
+                                 d_ext + 4 * (size_t)d0, false));
+    CENTRE_CUDA(ctx, cudaEventRecord(done_ev, ctx->stream));
+    CENTRE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, done_ev, 0));
+    CENTRE_CUDA(ctx, cudaMemcpyAsync(bins + d0 * fout, d_out + d0 * fout, (d1 - d0) * fout,
+                                     cudaMemcpyDeviceToHost, ctx->copy_out));
+    CENTRE_CUDA(ctx, cudaMemcpyAsync(extremes + 4 * (size_t)d0, d_ext + 4 * (size_t)d0,
+                                     32 * (size_t)(d1 - d0), cudaMemcpyDeviceToHost, ctx->copy_out));
+  }
+  CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->copy_out));
   CENTRE_TRY(read_flag(ctx));
-  CENTRE_CUDA(ctx, cudaMemcpyAsync(bins, d_out, nbins, cudaMemcpyDeviceToHost, ctx->stream));
-  CENTRE_CUDA(ctx, cudaMemcpyAsync(extremes, d_ext, 32 * (size_t)ndof, cudaMemcpyDeviceToHost,
-                                   ctx->stream));
-  CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return CENTRE_OK;
 }
 

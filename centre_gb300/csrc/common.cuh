@@ -38,6 +38,10 @@ struct centre_ctx {
   std::string last_error;
   centre::DevBuf scratch[9];   // one per ScratchSlot (below)
   int *d_flag = nullptr;   // device error flag (bin range, timeouts)
+  // copy-in and copy-out streams and their events for the host-pointer
+  // entry points that overlap transfers with kernels (created on first use)
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t copy_ev[16] = {};
   int *h_flag = nullptr;   // pinned mirror
   int cc_major = 0, cc_minor = 0;
   // fixed-point c ln c tables (2^16 entries), one per moment scale s in use

@@ -849,7 +849,8 @@ void host_fit_thresholds(int nfit, double bs, float *t) {
 
 int launch_discretize(centre_ctx *ctx, int bat_type, const float *d_data, uint32_t ndof,
                       uint64_t nframes, const uint8_t *schemes, uint32_t nschemes,
-                      uint8_t bins_ref, int optimize, uint8_t *d_bins, double *d_ext) {
+                      uint8_t bins_ref, int optimize, uint8_t *d_bins, double *d_ext,
+                      bool reset_flag) {
   if (bat_type < 1 || bat_type > 3) return set_error(ctx, CENTRE_E_ARG, "bad BAT type");
   if (nschemes < 1 || nschemes > (uint32_t)kMaxSchemes)
     return set_error(ctx, CENTRE_E_ARG, "nschemes must be 1..16");
@@ -897,7 +898,7 @@ int launch_discretize(centre_ctx *ctx, int bat_type, const float *d_data, uint32
   CENTRE_CUDA(ctx, cudaFuncSetAttribute(discretize_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
-  CENTRE_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+  if (reset_flag) CENTRE_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
 
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(ndof * csize), 1, 1);

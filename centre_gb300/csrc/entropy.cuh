@@ -162,7 +162,8 @@ int launch_entropy2d_counts(centre_ctx *ctx, const EntParams &P, int scheme,
 // discretize.cu
 int launch_discretize(centre_ctx *ctx, int bat_type, const float *d_data, uint32_t ndof,
                       uint64_t nframes, const uint8_t *schemes, uint32_t nschemes,
-                      uint8_t bins_ref, int optimize, uint8_t *d_bins, double *d_ext);
+                      uint8_t bins_ref, int optimize, uint8_t *d_bins, double *d_ext,
+                      bool reset_flag = true);
 
 // vmkde.cu
 int launch_vmkde(centre_ctx *ctx, const float *d_data, uint32_t ndof, uint64_t nframes,
