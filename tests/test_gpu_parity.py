@@ -246,8 +246,9 @@ def test_pair_counts_report_bad_bin_of_any_thread(gpu):
 def test_pair_counts_of_concentrated_cells(gpu, orc, nframes, nsteps):
     """Histogram-form moments on cells far past the shared c ln c table and
     past 2^16 counts (three DOFs nearly constant, one exactly constant), with
-    one step of 100,000 frames and with many short steps, on a frame count
-    that is not a multiple of 4 (the byte path): equal to the oracle's."""
+    one step of 100,000 frames and with many short steps, and on a frame count
+    that is not a multiple of 4 (rows off word boundaries, read through the
+    funnel-shifted 32-bit loads): equal to the oracle's."""
     rng = np.random.default_rng(nframes + nsteps)
     nb = 50
     bins = rng.integers(0, nb, (7, 1, nframes), dtype=np.uint8)
