@@ -540,35 +540,49 @@ int centre_gpu_discretize(centre_ctx *ctx, int bat_type, const float *data, uint
   // stream out on three streams, so the transfers overlap the kernels (and
   // each other) instead of running before and after them
   CENTRE_TRY(copy_streams(ctx));
+  // Every path below ends by waiting for all three streams: copies that read
+  // the caller's BAT or write its bins must not outlive the call, also when
+  // a step fails part way.
+  int rc = CENTRE_OK;
+  auto step = [&](cudaError_t e, const char *what) {
+    if (rc == CENTRE_OK && e != cudaSuccess) rc = check_cuda(ctx, e, what);
+    return rc == CENTRE_OK;
+  };
   // one flag for all chunks: the chunk launches do not reset it
-  CENTRE_CUDA(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+  step(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream), "flag reset");
   // the first upload waits for work already queued on the context's stream
   // (it may still read the scratch the upload fills)
-  CENTRE_CUDA(ctx, cudaEventRecord(ctx->copy_ev[15], ctx->stream));
-  CENTRE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_in, ctx->copy_ev[15], 0));
+  step(cudaEventRecord(ctx->copy_ev[15], ctx->stream), "event");
+  step(cudaStreamWaitEvent(ctx->copy_in, ctx->copy_ev[15], 0), "stream wait");
   const uint32_t nchunk = ndof >= 4 * kDiscChunkMinDofs ? 4u : 1u;
-  for (uint32_t c = 0; c < nchunk; ++c) {
+  const size_t fin = (size_t)nframes * 4, fout = (size_t)nschemes * nframes;
+  for (uint32_t c = 0; c < nchunk && rc == CENTRE_OK; ++c) {
     const uint32_t d0 = (uint32_t)((uint64_t)ndof * c / nchunk);
     const uint32_t d1 = (uint32_t)((uint64_t)ndof * (c + 1) / nchunk);
-    const size_t fin = (size_t)nframes * 4, fout = (size_t)nschemes * nframes;
     cudaEvent_t in_ev = ctx->copy_ev[2 * c], done_ev = ctx->copy_ev[2 * c + 1];
-    CENTRE_CUDA(ctx, cudaMemcpyAsync(d_in + d0 * fin, data + (size_t)d0 * nframes,
-                                     (d1 - d0) * fin, cudaMemcpyHostToDevice, ctx->copy_in));
-    CENTRE_CUDA(ctx, cudaEventRecord(in_ev, ctx->copy_in));
-    CENTRE_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, in_ev, 0));
-    CENTRE_TRY(launch_discretize(ctx, bat_type, (const float *)(d_in + d0 * fin), d1 - d0, nframes,
-                                 bin_schemes, nschemes, bins_ref, optimize_dih, d_out + d0 * fout,
-                                 d_ext + 4 * (size_t)d0, false));
-    CENTRE_CUDA(ctx, cudaEventRecord(done_ev, ctx->stream));
-    CENTRE_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, done_ev, 0));
-    CENTRE_CUDA(ctx, cudaMemcpyAsync(bins + d0 * fout, d_out + d0 * fout, (d1 - d0) * fout,
-                                     cudaMemcpyDeviceToHost, ctx->copy_out));
-    CENTRE_CUDA(ctx, cudaMemcpyAsync(extremes + 4 * (size_t)d0, d_ext + 4 * (size_t)d0,
-                                     32 * (size_t)(d1 - d0), cudaMemcpyDeviceToHost, ctx->copy_out));
+    if (!step(cudaMemcpyAsync(d_in + d0 * fin, data + (size_t)d0 * nframes, (d1 - d0) * fin,
+                              cudaMemcpyHostToDevice, ctx->copy_in), "BAT upload") ||
+        !step(cudaEventRecord(in_ev, ctx->copy_in), "event") ||
+        !step(cudaStreamWaitEvent(ctx->stream, in_ev, 0), "stream wait"))
+      break;
+    rc = launch_discretize(ctx, bat_type, (const float *)(d_in + d0 * fin), d1 - d0, nframes,
+                           bin_schemes, nschemes, bins_ref, optimize_dih, d_out + d0 * fout,
+                           d_ext + 4 * (size_t)d0, false);
+    if (rc != CENTRE_OK) break;
+    if (!step(cudaEventRecord(done_ev, ctx->stream), "event") ||
+        !step(cudaStreamWaitEvent(ctx->copy_out, done_ev, 0), "stream wait") ||
+        !step(cudaMemcpyAsync(bins + d0 * fout, d_out + d0 * fout, (d1 - d0) * fout,
+                              cudaMemcpyDeviceToHost, ctx->copy_out), "bins download") ||
+        !step(cudaMemcpyAsync(extremes + 4 * (size_t)d0, d_ext + 4 * (size_t)d0,
+                              32 * (size_t)(d1 - d0), cudaMemcpyDeviceToHost, ctx->copy_out),
+              "extremes download"))
+      break;
   }
-  CENTRE_CUDA(ctx, cudaStreamSynchronize(ctx->copy_out));
-  CENTRE_TRY(read_flag(ctx));
-  return CENTRE_OK;
+  step(cudaStreamSynchronize(ctx->copy_in), "copy-in sync");
+  step(cudaStreamSynchronize(ctx->stream), "stream sync");
+  step(cudaStreamSynchronize(ctx->copy_out), "copy-out sync");
+  if (rc != CENTRE_OK) return rc;
+  return read_flag(ctx);
 }
 
 // ---- 1-D -------------------------------------------------------------------

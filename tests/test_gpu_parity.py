@@ -59,6 +59,25 @@ def test_discretize_synthetic_vs_oracle(gpu, orc, nframes):
                 np.testing.assert_allclose(ge[:, 2], oe[:, 2], rtol=1e-12)
 
 
+def test_discretize_chunked_transfers_vs_oracle(gpu, orc):
+    """Blocks of 256 DOFs and more go through the host entry in four chunks
+    whose transfers overlap the binning: bins and extremes equal the
+    oracle's, and a value out of domain in the last chunk fails the call."""
+    tr = chain_trajectory(300, 20_001, seed=77)
+    for typ, blk in tr.blocks():
+        gb, ge = gpu.discretize(typ, blk, [50, 7], bins_ref=50, optimize=True)
+        ob, oe = orc.discretize(typ, blk, [50, 7], bins_ref=50, optimize=True)
+        assert blk.shape[0] >= 256
+        assert np.array_equal(gb, ob), typ
+        assert np.array_equal(ge[:, [0, 1, 3]], oe[:, [0, 1, 3]])
+        np.testing.assert_allclose(ge[:, 2], oe[:, 2], rtol=1e-12)
+    bad = np.array(tr.blocks()[2][1])
+    bad[290, 17] = 7.0   # torsion >= 2pi
+    with pytest.raises(CentreError) as e:
+        gpu.discretize(3, bad, [50], bins_ref=50, optimize=True)
+    assert e.value.status == -1
+
+
 def test_discretize_edge_values_vs_oracle(gpu, orc):
     """Signed zeros, exact zeros, constant DOFs, wide uniform ranges and
     values on a single float: the binning table's edge cases."""
