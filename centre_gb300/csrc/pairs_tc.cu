@@ -7,47 +7,60 @@
 //
 // Formulation.  Rows of the one-hot matrix O are (DOF, bin) packed without
 // padding: row = dof * nb + bin.  O[frame][row] = 2 when DOF's bin at frame is
-// bin, else 0.  The joint counts of every pair are blocks of O^T O / 4.  A CTA
-// computes a 128 x 256 tile of O^T O (rows [rb, rb+128), columns [cb,
-// cb+256)) over all frames with tcgen05.mma kind::f8f6f4 (E4M3 operands, FP32
-// accumulator in TMEM): 2.0 and 0.0 are exact in E4M3 and FP32 sums of
-// multiples of 4 up to 2^24 are exact, so the counts are exact for up to
-// 2^22 frames.
+// bin, else 0.  The joint counts of every pair are blocks of O^T O / 4.  A
+// pair of CTAs (a cluster of two on one TPC) computes a 256 x 256 tile of
+// O^T O over all frames with tcgen05.mma.cta_group::2 kind::f8f6f4 (E4M3
+// operands, FP32 accumulator in TMEM; M = 256, N = 256, K = 32): CTA r holds
+// A rows [rb + 128r, +128), B rows (tile columns) [cb + 128r, +128) and the
+// accumulator rows of its A half, all 256 columns.  2.0 and 0.0 are exact in
+// E4M3 and FP32 sums of multiples of 4 up to 2^24 are exact, so the counts are
+// exact for up to 2^22 frames.  Against one CTA per 128 x 256 tile, each SM
+// builds 256 instead of 384 operand rows per 128 frames and its tensor core
+// reads 2/3 of the operand bytes for the same accumulator area.
 //
 // Operands.  The frame axis is cut into 128-frame blocks (one 128-byte
 // K-major row of an operand tile); a block that holds the end of a
 // convergence step is used twice, once per side of the step boundary (a
-// "piece" is a block and a frame range inside it).  A loader warp stages the
-// bins of the tile's DOFs for each piece with two TMA loads
-// (cp.async.bulk.tensor.2d: the 9 DOF rows of the A tile and the 17 of the B
-// tile, 128 frames each) into a six-deep ring.  Twelve producer warps then
-// rewrite the whole operand stage (128 + 256 rows x 128 bytes, 128-byte
-// swizzled) from those bins: lane (g, s) of warp w owns segment g (16 frames)
-// of the 8 rows 32w + 8s .. +7 of the stage, in every piece, so no producer
-// ever writes where another does and no stage needs clearing.  For each row
-// it compares the 16 bins of its DOF with the row's bin four at a time with
-// integer arithmetic (no per-byte work) and writes the 16 one-hot bytes with
-// one 128-bit shared store; the stores of one instruction hit the eight
-// 16-byte bank groups of a swizzled row group once each.  Frames of a piece's
-// block outside the piece are zeroed in the A operand only.
+// "piece" is a block and a frame range inside it).  In each CTA a loader warp
+// stages the bins of its halves' DOFs for each piece with two TMA loads
+// (cp.async.bulk.tensor.2d: 9 DOF rows for the A half, 9 for the B half, 128
+// frames each) into a 16-slot ring.  Producer warps then rewrite the CTA's
+// whole operand stage (128 + 128 rows x 128 bytes, 128-byte swizzled) from
+// those bins: lane (g, s) owns segment g (16 frames) of 8 rows of a 32-row
+// group, in every piece the warp's stage takes, so no producer ever writes
+// where another does and no stage needs clearing.  For each row it compares
+// the 16 bins of its DOF with the row's bin four at a time with integer
+// arithmetic (no per-byte work) and writes the 16 one-hot bytes with one
+// 128-bit shared store; the stores of one instruction hit the eight 16-byte
+// bank groups of a swizzled row group once each.  Frames of a piece's block
+// outside the piece are zeroed in the A operand only.
+//
+// Pair protocol.  The even CTA's full barrier of a stage counts the producer
+// lanes of both CTAs (the odd CTA arrives through its shared::cluster
+// address); its MMA thread issues the pair's MMAs and commits the stage's and
+// the accumulator's release to both CTAs at once (multicast).  Both CTAs
+// allocate TMEM together (cta_group::2: the same columns in both SMs), meet
+// on a cluster barrier after initialising their barriers and again before
+// freeing TMEM.
 //
 // Accumulation.  Convergence steps are prefixes of the frame axis.  The MMAs
 // of a step accumulate into TMEM columns [256, 512) starting from zero; at the
-// step's end the epilogue warps add them to the cumulative counts in columns
-// [0, 256) and release the accumulator at once, so the next step's MMAs
-// overlap the rest of the epilogue: reading the cumulative counts
-// (tcgen05.ld), reducing each (row DOF, column DOF) block to sum F(c) (the
-// 64-bit fixed-point c ln c of entropy.cuh) and the non-empty cell count, and
-// adding them into the pair's moments with integer atomics (tiles split pair
-// blocks; integer addition keeps the result independent of the split).
+// step's end the epilogue warps of each CTA add them to the cumulative counts
+// in columns [0, 256) and release the accumulator (to the even CTA's
+// barrier) at once, so the next step's MMAs overlap the rest of the epilogue:
+// reading the cumulative counts (tcgen05.ld), reducing each (row DOF, column
+// DOF) block to sum F(c) (the 64-bit fixed-point c ln c of entropy.cuh) and
+// the non-empty cell count, and adding them into the pair's moments with
+// integer atomics (tiles split pair blocks; integer addition keeps the result
+// independent of the split).
 //
-// Warp roles (704 threads): warp 0 allocates TMEM and one lane issues the
-// MMAs; one lane of warp 1 issues the TMA loads of the bins; warps 2-13
-// produce operand stages (four A row groups, eight B row groups); warps 14-21
-// run the epilogue as two quartets over the two column halves (TMEM lane group
-// = warp % 4).  Every mbarrier wait is bounded: on expiry the kernel sets an
-// error flag, lets the MMAs and loads it issued drain (again bounded), frees
-// its TMEM and returns.
+// Warp roles (640 threads per CTA): warp 0 allocates TMEM and, in the even
+// CTA, one lane issues the MMAs; one lane of warp 1 issues the TMA loads of
+// the bins; warps 2-11 produce operand stages (two per stage, four 32-row
+// groups each); warps 12-19 run the epilogue as two quartets over the two
+// column halves (TMEM lane group = warp % 4).  Every mbarrier wait is
+// bounded: on expiry the kernel sets an error flag, lets the MMAs and loads it
+// issued drain (again bounded), frees its TMEM and returns.
 //
 // Bins outside [0, nb) never steer an address here (the operand stores go to
 // fixed places); a check pass ahead of the contraction reports them.
@@ -63,25 +76,28 @@
 namespace centre {
 namespace {
 
-constexpr int kTileM = 128;                 // A rows (row DOF bins)
-constexpr int kTileN = 256;                 // B rows (column DOF bins)
+constexpr int kPairM = 256;                 // tile rows (A rows of both CTAs)
+constexpr int kHalfM = 128;                 // A rows of one CTA (its TMEM lanes)
+constexpr int kTileN = 256;                 // tile columns (B rows of both CTAs)
+constexpr int kHalfN = 128;                 // B rows of one CTA
 constexpr int kChunk = 128;                 // frames per block (one 128 B row)
-constexpr int kStages = 4;
-constexpr int kABytes = kTileM * kChunk;    // 16 KB
-constexpr int kBBytes = kTileN * kChunk;    // 32 KB
+constexpr int kStages = 5;
+constexpr int kABytes = kHalfM * kChunk;    // 16 KB
+constexpr int kBBytes = kHalfN * kChunk;    // 16 KB
 constexpr int kStageBytes = kABytes + kBBytes;
 constexpr int kMinBins = 16;                // DOF slots per tile bounded below
-constexpr int kMaxSlotsA = kTileM / kMinBins + 1;  // 9
-constexpr int kMaxSlotsB = kTileN / kMinBins + 1;  // 17
-constexpr int kBinRows = kMaxSlotsA + kMaxSlotsB;  // DOF rows staged per piece
-constexpr int kBinBytes = kBinRows * kChunk;       // 3,328
-constexpr int kBinStages = 8;
+constexpr int kSlotsHalf = kHalfM / kMinBins + 1;  // 9 DOFs in 128 rows
+constexpr int kMaxSlotsA = kSlotsHalf;             // row DOFs of a CTA's A half
+constexpr int kMaxSlotsB = kTileN / kMinBins + 1;  // 17 column DOFs of a tile
+constexpr int kBinRows = 2 * kSlotsHalf;           // DOF rows staged per piece
+constexpr int kBinBytes = kBinRows * kChunk;       // 2,304
+constexpr int kBinStages = 16;
 constexpr int kTabTc = 512;                 // fixed-point c ln c entries in shared memory
-constexpr int kGroupsA = kTileM / 32;       // 32-row groups of the A operand
-constexpr int kRowGroups = (kTileM + kTileN) / 32;   // 32-row groups of a stage
+constexpr int kGroupsA = kHalfM / 32;       // 32-row groups of the A half
+constexpr int kRowGroups = (kHalfM + kHalfN) / 32;   // 32-row groups of a stage
 // Producer warps: a team of kPerTeam warps per operand stage, each warp
 // rewriting kGroupsPerWarp row groups of every piece its stage takes.
-constexpr int kPerTeam = 3;
+constexpr int kPerTeam = 2;
 constexpr int kGroupsPerWarp = kRowGroups / kPerTeam;
 constexpr int kProducers = kStages * kPerTeam;
 // Epilogue: kEpiGroups warp quartets, quartet g reading accumulator columns
@@ -102,7 +118,7 @@ constexpr uint32_t kIncCol = 256;
 constexpr long long kWaitCycles = 20000000000ll;  // ~10 s at 2 GHz
 
 struct TcParams {
-  const uint2 *tiles;     // (row tile, column tile)
+  const uint2 *tiles;     // (row tile of 256, column tile of 256)
   uint64_t ntiles;
   uint64_t step_size;
   uint32_t ndof;
@@ -112,20 +128,26 @@ struct TcParams {
   int fix_scale;          // moment scale s (counts beyond the table)
 };
 
-// Geometry of one 128 x 256 tile of O^T O.
+// Geometry of a CTA's half of one 256 x 256 tile of O^T O: its 128 A rows
+// (the accumulator rows in its TMEM) and 128 B rows, and the tile's 256
+// columns (the accumulator columns of both CTAs).
 struct StageMeta {
-  int rb, cb;       // tile rows / columns base
-  int d0a, nda;     // first DOF and DOF count of the A tile
-  int d0b, ndb;
+  int rb;           // first row of this CTA's A half
+  int cb;           // first column of the tile
+  int cbh;          // first row of this CTA's B half (= a column)
+  int d0a;          // first DOF of the A half
+  int d0b;          // first DOF of the tile's columns
+  int d0bh;         // first DOF of the B half
 };
 
 struct Smem {
-  uint64_t full[kStages];      // operand stage built (all producer lanes)
+  uint64_t full[kStages];      // operand stage built (producer lanes of both CTAs;
+                               // the even CTA's is the one used)
   uint64_t empty[kStages];     // operand stage consumed (MMA commit)
   uint64_t bfull[kBinStages];  // bins of a piece landed (TMA bytes)
   uint64_t bempty[kBinStages]; // bins of a piece read (all producer lanes)
   uint64_t accfull;
-  uint64_t accempty;
+  uint64_t accempty;           // both CTAs' epilogue threads (the even CTA's)
   uint64_t drain;
   uint32_t tmem_base;
   int abort_flag;
@@ -153,7 +175,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   // spinning, which leaves the issue slots to the warps doing work
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}\n"
       : "=r"(ok)
       : "r"(smem_u32(bar)), "r"(parity), "r"(20000u)
@@ -185,8 +207,11 @@ __device__ bool wait_bar(Smem &S, uint64_t *bar, uint32_t parity, int *flag) {
   }
   return true;
 }
+// Generic-proxy writes of this thread to shared memory become visible to the
+// tensor cores of both CTAs of the pair (the MMA reads each CTA's operand
+// halves).
 __device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cluster;" ::: "memory");
 }
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -210,16 +235,18 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
-// Instruction descriptor: D = F32, A = B = E4M3, both K-major, N = 256, M = 128.
+// Instruction descriptor: D = F32, A = B = E4M3, both K-major, N = 256,
+// M = 256 (the CTA pair: each CTA holds 128 rows of A, 128 rows of B and 128
+// rows of D).
 constexpr uint32_t kIdesc = (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(kTileN >> 3) << 17) |
-                            ((uint32_t)(kTileM >> 4) << 24);
+                            ((uint32_t)(kPairM >> 4) << 24);
 
 __device__ __forceinline__ void mma_f8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
                                        uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
       "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
       : "memory");
 }
@@ -265,10 +292,42 @@ __device__ __forceinline__ void tmem_wait_ld_w(uint32_t (&v)[kEpiW]) {
                :
                : "memory");
 }
-__device__ __forceinline__ void mma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+// Arrive on `bar` in both CTAs of the pair once every MMA issued so far has
+// completed.
+__device__ __forceinline__ void mma_commit_both(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+      "[%0], %1;" ::"r"(smem_u32(bar)),
+      "h"((unsigned short)3)
+      : "memory");
+}
+// The same, on this CTA's `bar` only.
+__device__ __forceinline__ void mma_commit_local(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                    smem_u32(bar))
                : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Address of this CTA's shared variable `p` in the even CTA of the pair.
+__device__ __forceinline__ uint32_t leader_addr(const void *p) {
+  uint32_t a;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, 0;" : "=r"(a) : "r"(smem_u32(p)));
+  return a;
+}
+// Arrive on an mbarrier of the pair (a shared::cluster address).
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t caddr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(caddr)
+               : "memory");
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile(
+      "barrier.cluster.arrive.release.aligned;\n\t"
+      "barrier.cluster.wait.acquire.aligned;" ::
+          : "memory");
 }
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
@@ -360,15 +419,14 @@ struct PieceWalker {
   }
 };
 
-__device__ __forceinline__ void tile_geometry(const TcParams &P, uint2 tl, StageMeta &m) {
-  m.rb = (int)tl.x * kTileM;
+__device__ __forceinline__ void tile_geometry(const TcParams &P, uint2 tl, uint32_t rank,
+                                              StageMeta &m) {
+  m.rb = (int)tl.x * kPairM + (int)rank * kHalfM;
   m.cb = (int)tl.y * kTileN;
+  m.cbh = m.cb + (int)rank * kHalfN;
   m.d0a = m.rb / P.nb;
-  const int lasta = min((int)P.nrows, m.rb + kTileM) - 1;
-  m.nda = lasta / P.nb - m.d0a + 1;
   m.d0b = m.cb / P.nb;
-  const int lastb = min((int)P.nrows, m.cb + kTileN) - 1;
-  m.ndb = lastb / P.nb - m.d0b + 1;
+  m.d0bh = m.cbh / P.nb;
 }
 
 // F(c) for counts beyond the global table (rare).  Kept out of line so the
@@ -447,6 +505,10 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
   const uint32_t bins_s = stages_s + (uint32_t)(kStages * kStageBytes);
   Smem &S = *reinterpret_cast<Smem *>(stages + kStages * kStageBytes + kBinStages * kBinBytes);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // the CTA pair (a cluster of two) walks the pair's tiles; the even CTA
+  // issues the MMAs
+  const uint32_t rank = cluster_rank();
+  const uint32_t pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
 
   // ---- set-up ------------------------------------------------------------
   for (int i = tid; i < kTabTc; i += kThreads) S.tab[i] = gfix[i];
@@ -456,7 +518,7 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
   }
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
-      mbar_init(&S.full[s], 32 * kPerTeam);
+      mbar_init(&S.full[s], 2 * 32 * kPerTeam);
       mbar_init(&S.empty[s], 1);
     }
     for (int s = 0; s < kBinStages; ++s) {
@@ -464,55 +526,63 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
       mbar_init(&S.bempty[s], 32 * kPerTeam);
     }
     mbar_init(&S.accfull, 1);
-    mbar_init(&S.accempty, kEpilogue);
+    mbar_init(&S.accempty, 2 * kEpilogue);
     mbar_init(&S.drain, 1);
     S.abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   fence_proxy_async();
   if (warp == kWarpMma) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+    // one warp in each CTA of the pair allocates, together: the same
+    // columns in both SMs
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&S.tmem_base)),
                  "r"(kTmemCols)
                  : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
   }
   tc_fence_before();
   __syncthreads();
+  // both CTAs' barriers are initialised before either arrives on the other's
+  cluster_sync();
   tc_fence_after();
   const uint32_t tmem = S.tmem_base;
 
   if (warp == kWarpMma) {
-    // ---- MMA issuer --------------------------------------------------------
-    if (lane == 0) {
+    // ---- MMA issuer (the even CTA) ------------------------------------------
+    if (lane == 0 && rank == 0) {
       PieceWalker walk;
-      walk.start(blockIdx.x, gridDim.x, (uint32_t)P.ntiles, (uint32_t)P.step_size, P.nsteps);
+      walk.start(pair, npairs, (uint32_t)P.ntiles, (uint32_t)P.step_size, P.nsteps);
       int s = 0;
       uint32_t ph = 0;
       uint32_t nsnap = 0;
       bool issued = false;
       bool first = true;
+      // descriptors of stage 0's halves; a stage adds kStageBytes and a K
+      // step 32 bytes to the start-address field (16-byte units, no carry
+      // out of its 14 bits below 256 KB)
+      const uint64_t desc0 = sw128_desc(stages_s);
       for (;;) {
         const Piece pc = walk.next();
         if (!pc.valid) break;
         if (!wait_bar(S, &S.full[s], ph, flag)) break;
         tc_fence_after();
-        const uint32_t a0 = stages_s + (uint32_t)(s * kStageBytes);
-        const uint32_t b0 = a0 + kABytes;
+        const uint64_t da = desc0 + (uint64_t)(s * (kStageBytes >> 4));
+        const uint64_t db = da + (uint64_t)(kABytes >> 4);
         // the K steps (32 frames each) the piece touches
         const int k0 = pc.lo >> 5, k1 = (pc.hi + 31) >> 5;
         for (int k = k0; k < k1; ++k)
-          mma_f8(tmem + kIncCol, sw128_desc(a0 + 32u * k), sw128_desc(b0 + 32u * k),
+          mma_f8(tmem + kIncCol, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k),
                  (first && k == k0) ? 0u : 1u);
         issued = true;
         first = false;
-        mma_commit(&S.empty[s]);
+        mma_commit_both(&S.empty[s]);
         if (++s == kStages) {
           s = 0;
           ph ^= 1u;
         }
         if (pc.last) {
-          mma_commit(&S.accfull);
+          mma_commit_both(&S.accfull);
           ++nsnap;
           // wait until the epilogue has added this step's counts to the
           // cumulative ones; the next step starts from zero
@@ -523,7 +593,7 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
       }
       if (issued) {
         // drain: every MMA issued by this thread has completed
-        mma_commit(&S.drain);
+        mma_commit_local(&S.drain);
         wait_landed(&S.drain, 0, flag);
       }
     }
@@ -532,7 +602,7 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
     // ---- bins loader -------------------------------------------------------
     if (lane == 0) {
       PieceWalker walk;
-      walk.start(blockIdx.x, gridDim.x, (uint32_t)P.ntiles, (uint32_t)P.step_size, P.nsteps);
+      walk.start(pair, npairs, (uint32_t)P.ntiles, (uint32_t)P.step_size, P.nsteps);
       int bs = 0;
       uint32_t round = 0;        // uses of the ring so far, per slot
       uint32_t tile = ~0u;
@@ -545,15 +615,15 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
         if (round > 0 && !wait_bar<128>(S, &S.bempty[bs], (round - 1) & 1u, flag)) break;
         if (pc.ti != tile) {
           StageMeta m;
-          tile_geometry(P, P.tiles[pc.ti], m);
+          tile_geometry(P, P.tiles[pc.ti], rank, m);
           d0a = m.d0a;
-          d0b = m.d0b;
+          d0b = m.d0bh;
           tile = pc.ti;
         }
         const uint32_t dst = bins_s + (uint32_t)(bs * kBinBytes);
         mbar_expect_tx(&S.bfull[bs], kBinBytes);
         tma_load_2d(dst, &map_a, (int)(pc.blk * kChunk), d0a, &S.bfull[bs]);
-        tma_load_2d(dst + kMaxSlotsA * kChunk, &map_b, (int)(pc.blk * kChunk), d0b, &S.bfull[bs]);
+        tma_load_2d(dst + kSlotsHalf * kChunk, &map_b, (int)(pc.blk * kChunk), d0b, &S.bfull[bs]);
         ++n;
         if (++bs == kBinStages) {
           bs = 0;
@@ -569,9 +639,10 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
     __syncwarp();
   } else if (warp < kWarpEpi) {
     // ---- producers: the team of warps 2 + p, 2 + p + kStages, ... builds
-    // the pieces n with n % kStages == p into operand stage p; its warp h
-    // rewrites row groups h, h + kPerTeam, ... (groups 0-3 the A tile, 4-11
-    // the B tile), lane (g, s) segment g of rows 32 * group + 8s .. + 7
+    // the pieces n with n % kStages == p into operand stage p of this CTA;
+    // its warp h rewrites row groups h, h + kPerTeam, ... (groups 0-3 the A
+    // half, 4-7 the B half), lane (g, s) segment g of rows 32 * group + 8s
+    // .. + 7
     const int pw = warp - kWarpProd;
     const int team = pw % kStages;
     const int h = pw / kStages;
@@ -587,20 +658,20 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
     uint32_t lds0[kGroupsPerWarp], lds1[kGroupsPerWarp];
     auto geometry = [&](uint32_t ti) {
       StageMeta m;
-      tile_geometry(P, P.tiles[ti], m);
+      tile_geometry(P, P.tiles[ti], rank, m);
 #pragma unroll
       for (int k = 0; k < kGroupsPerWarp; ++k) {
         const int rg = h + kPerTeam * k;
         const bool isA = rg < kGroupsA;
-        const int r0 = (isA ? m.rb + 32 * rg : m.cb + 32 * (rg - kGroupsA)) + sub8;
+        const int r0 = (isA ? m.rb + 32 * rg : m.cbh + 32 * (rg - kGroupsA)) + sub8;
         const int dof0 = r0 / nb;
         bin0[k] = r0 - dof0 * nb;
         split[k] = nb - bin0[k];
-        // staged DOF rows: the A tile's from row 0, the B tile's from row
-        // kMaxSlotsA; rows past the matrix read the zero fill
-        const int first = isA ? 0 : kMaxSlotsA;
-        const int lastrow = isA ? kMaxSlotsA - 1 : kBinRows - 1;
-        const int slot = min(first + dof0 - (isA ? m.d0a : m.d0b), lastrow);
+        // staged DOF rows: the A half's from row 0, the B half's from row
+        // kSlotsHalf; rows past the matrix read the zero fill
+        const int first = isA ? 0 : kSlotsHalf;
+        const int lastrow = isA ? kSlotsHalf - 1 : kBinRows - 1;
+        const int slot = min(first + dof0 - (isA ? m.d0a : m.d0bh), lastrow);
         lds0[k] = (uint32_t)slot * kChunk + g16;
         lds1[k] = (uint32_t)min(slot + 1, lastrow) * kChunk + g16;
       }
@@ -614,9 +685,11 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
       return go != 0;
     };
     PieceWalker walk;
-    walk.start(blockIdx.x, gridDim.x, (uint32_t)P.ntiles, (uint32_t)P.step_size, P.nsteps);
+    walk.start(pair, npairs, (uint32_t)P.ntiles, (uint32_t)P.step_size, P.nsteps);
     Piece pc;
     for (int i = 0; i <= team; ++i) pc = walk.next();
+    // this stage's full barrier in the even CTA
+    const uint32_t full_pair = leader_addr(&S.full[team]);
     uint32_t n = (uint32_t)team;   // index of the piece among the CTA's pieces
     uint32_t tile = ~0u;
     uint32_t use = 0;              // earlier pieces built into this stage
@@ -657,7 +730,7 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
       // loader's next copy into the slot
       mbar_arrive(&S.bempty[bs]);
       fence_proxy_async();
-      mbar_arrive(&S.full[team]);
+      mbar_arrive_cluster(full_pair);
       ++use;
       for (int i = 0; i < kStages; ++i) pc = walk.next();
       n += kStages;
@@ -671,9 +744,11 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
     uint32_t nsnap = 0;
     bool ok = true;
     const int nb = P.nb;
-    for (uint64_t ti = blockIdx.x; ti < P.ntiles && ok; ti += gridDim.x) {
+    // the accumulator's release goes to the even CTA's barrier
+    const uint32_t accempty_pair = leader_addr(&S.accempty);
+    for (uint64_t ti = pair; ti < P.ntiles && ok; ti += npairs) {
       StageMeta m;
-      tile_geometry(P, P.tiles[ti], m);
+      tile_geometry(P, P.tiles[ti], rank, m);
       const int grow = m.rb + etid;
       const int rd = grow / nb;
       const bool rowvalid = grow < (int)P.nrows;
@@ -711,7 +786,7 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
         }
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         tc_fence_before();
-        mbar_arrive(&S.accempty);
+        mbar_arrive_cluster(accempty_pair);
         // Each thread reads its row of the cumulative counts in chunks of 8
         // columns and sums the exact c ln c of its cells per column DOF in
         // registers.  At each column DOF boundary the rows of one row DOF
@@ -826,9 +901,13 @@ pairs_tc_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant
   // ---- tear-down -----------------------------------------------------------
   tc_fence_before();
   __syncthreads();
+  // the pair leaves together: the even CTA's MMAs read this CTA's operands
+  // and write its TMEM until they drain, and the odd CTA arrives on the even
+  // CTA's barriers until its last piece
+  cluster_sync();
   if (warp == kWarpMma) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(kTmemCols)
                  : "memory");
   }
@@ -878,8 +957,8 @@ size_t tc_smem_bytes() {
 }
 static_assert(1024 + kStages * kStageBytes + kBinStages * kBinBytes + sizeof(Smem) <= 232448,
               "shared memory of the tensor-core count kernel above 227 KB");
-static_assert(kThreads == 704 && kRowGroups == kPerTeam * kGroupsPerWarp, "warp roles");
-static_assert((kBinStages & (kBinStages - 1)) == 0 && kBinStages % kStages == 0, "bins ring");
+static_assert(kThreads == 640 && kRowGroups == kPerTeam * kGroupsPerWarp, "warp roles");
+static_assert((kBinStages & (kBinStages - 1)) == 0, "bins ring slots: a power of two");
 
 template <int kMode, bool kSplit>
 int launch_tc(centre_ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, const TcParams &P,
@@ -889,9 +968,23 @@ int launch_tc(centre_ctx *ctx, const CUtensorMap &ma, const CUtensorMap &mb, con
   const size_t smem = tc_smem_bytes();
   CENTRE_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
+  // clusters of two CTAs (the pair of one MMA)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid, 1, 1);
+  cfg.blockDim = dim3(kThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   {
     KernelTimer kt(ctx, CENTRE_TIMER_PAIRS);
-    kern<<<grid, kThreads, smem, ctx->stream>>>(ma, mb, P, d_fix, d_sclnc, d_nnz, ctx->d_flag);
+    CENTRE_CUDA(ctx, cudaLaunchKernelEx(&cfg, kern, ma, mb, P, d_fix, d_sclnc, d_nnz,
+                                        ctx->d_flag));
   }
   ctx->launches++;
   CENTRE_CUDA(ctx, cudaGetLastError());
@@ -915,11 +1008,11 @@ int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const unsigned long l
   const uint64_t nrows = (uint64_t)ndof * nb;
   if (nrows >= (1ull << 31)) return set_error(ctx, CENTRE_E_UNSUPPORTED, "too many DOF bins");
   // tiles (row tile, column tile) holding at least one pair i < j
-  const int ntr = (int)((nrows + kTileM - 1) / kTileM);
+  const int ntr = (int)((nrows + kPairM - 1) / kPairM);
   const int ntc = (int)((nrows + kTileN - 1) / kTileN);
   std::vector<uint2> tiles;
   for (int a = 0; a < ntr; ++a) {
-    const int mind = (a * kTileM) / nb;
+    const int mind = (a * kPairM) / nb;
     for (int b = 0; b < ntc; ++b) {
       const uint64_t lastrow = std::min<uint64_t>(nrows, (uint64_t)(b + 1) * kTileN) - 1;
       const int maxd = (int)(lastrow / nb);
@@ -957,8 +1050,8 @@ int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const unsigned long l
   {
     const cuuint64_t gdim[2] = {nframes, ndof};
     const cuuint64_t gstride[1] = {pitch};
-    const cuuint32_t box_a[2] = {(cuuint32_t)kChunk, (cuuint32_t)kMaxSlotsA};
-    const cuuint32_t box_b[2] = {(cuuint32_t)kChunk, (cuuint32_t)kMaxSlotsB};
+    const cuuint32_t box_a[2] = {(cuuint32_t)kChunk, (cuuint32_t)kSlotsHalf};
+    const cuuint32_t box_b[2] = {(cuuint32_t)kChunk, (cuuint32_t)kSlotsHalf};
     const cuuint32_t estride[2] = {1, 1};
     CUresult cr = encode(&ma, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t *>(base), gdim,
                          gstride, box_a, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -986,7 +1079,9 @@ int launch_pairs_tc(centre_ctx *ctx, const PairParams &PP, const unsigned long l
   P.nb = nb;
   P.nsteps = PP.nsteps;
   P.fix_scale = PP.fix_scale;
-  const unsigned grid = (unsigned)std::min<uint64_t>(tiles.size(), (uint64_t)ctx->sm_count);
+  // one CTA pair per two SMs
+  const unsigned grid =
+      2u * (unsigned)std::min<uint64_t>(tiles.size(), (uint64_t)(ctx->sm_count / 2));
   const bool split = nb % 8 != 0;   // a lane's 8 rows may span two DOFs
   if (nb <= 64)
     return split ? launch_tc<0, true>(ctx, ma, mb, P, grid, d_fix, d_sclnc, d_nnz)
