@@ -288,10 +288,10 @@ int entropy2d_dev(centre_ctx *ctx, const centre_entropy_params *p, uint32_t ndof
       const int form = p->counts_form;
       // AUTO takes the tensor-core contraction only where the histograms
       // do not fit shared memory (more than 217 bins; kTcAutoMaxBins is 0).
-      // Everywhere else the shared-memory histogram is as fast or faster: it
+      // Everywhere else the shared-memory histogram is about as fast or faster: it
       // does one increment per frame and pair where the contraction does
-      // B^2 multiply-adds (all pairs of 2994 DOFs x 100,000 frames: 124.6
-      // against 128 ms at 16 bins, 172.6 against 1,624 ms at 50).
+      // B^2 multiply-adds (all pairs of 2994 DOFs x 100,000 frames: 120.2
+      // against 118.7 ms at 16 bins, 172.6 against 1,423 ms at 50).
       const bool use_tc =
           all && tc_supported(ctx, nb, E.nframes) &&
           (form == CENTRE_COUNTS_TC ||

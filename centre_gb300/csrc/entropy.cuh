@@ -189,10 +189,10 @@ int launch_corr_gemm(centre_ctx *ctx, const void *X, uint32_t n, uint32_t K, uin
 // pairs_tc.cu
 bool tc_supported(centre_ctx *ctx, int nb, uint64_t nframes);
 // largest bin count at which AUTO prefers the tensor-core contraction over
-// a shared-memory histogram that fits (none: the histogram form is as fast or
-// faster at every bin count it covers, e.g. 124.6 vs 128 ms at 16 bins for the
-// 2994-DOF chain); AUTO takes the contraction only where the histograms do not
-// fit shared memory
+// a shared-memory histogram that fits (none: the two are within 2 % at 16 bins,
+// 120.2 vs 118.7 ms for the 2994-DOF chain, and the histogram is faster above
+// it); AUTO takes the contraction only where the histograms do not fit shared
+// memory
 constexpr int kTcAutoMaxBins = 0;
 int launch_pairs_tc(centre_ctx *ctx, const PairParams &P, const unsigned long long *d_fix,
                     unsigned long long *d_sclnc, unsigned *d_nnz);
