@@ -496,9 +496,9 @@ def test_tc_rejects_bins_out_of_range(gpu):
 @pytest.mark.parametrize("natoms,nframes,nsteps,nb", [
     (200, 20_000, 4, 50), (200, 12_000, 3, 16), (120, 10_000, 2, 30)])
 def test_tc_counts_many_tiles_per_cta(gpu, orc, natoms, nframes, nsteps, nb):
-    """Thousands of 128 x 256 tiles for 152 persistent CTAs: every CTA walks
-    many tiles, and its producer warps move their stages from tile to tile
-    (the 594-DOF chain at 50 bins gives about 13,600 tiles).  The moments
+    """Thousands of 256 x 256 tiles for 76 persistent CTA pairs: every pair
+    walks many tiles, and its producer warps move their stages from tile to
+    tile (the 594-DOF chain at 50 bins gives about 6,900 tiles).  The moments
     must equal the shared-memory histogram's bit for bit on every run, and a
     sample of pairs must equal the oracle's counts."""
     tr = chain_trajectory(natoms, nframes, seed=natoms + nb, coupling="block8")
