@@ -905,8 +905,7 @@ int launch_pairs_global(centre_ctx *ctx, const PairParams &P, const uint32_t *d_
 }
 
 // ----------------------------------------------------------------------------
-// S2 from the integer moments (ML, MM).  One thread per (pair, step) of a
-// scheme.
+// S2 from the integer moments (ML, MM), every step of one scheme.
 __global__ void finalize2d_kernel(const uint32_t *__restrict__ pairs, int all_pairs,
                                   uint32_t ndof, const double *__restrict__ logw,
                                   const double *__restrict__ lsum,
@@ -914,10 +913,17 @@ __global__ void finalize2d_kernel(const uint32_t *__restrict__ pairs, int all_pa
                                   const unsigned *__restrict__ nnz,
                                   const __grid_constant__ EntParams P, int scheme,
                                   uint64_t npairs, double *__restrict__ s2) {
-  const uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  if (idx >= npairs * P.nsteps) return;
-  const uint64_t p = idx / P.nsteps;
-  const int t = (int)(idx % P.nsteps);
+  // One thread per pair over all its steps: the pair is decoded once, and
+  // the per-step 1/n (the only divisions, FP64 being scarce here) and log n
+  // are formed once per block.
+  __shared__ double inv_n[256], log_n[256];
+  for (int t = threadIdx.x; t < P.nsteps; t += blockDim.x) {
+    inv_n[t] = 1.0 / ((t + 1.0) * (double)P.step_size);
+    log_n[t] = logw[(uint64_t)ndof * P.nschemes + t];
+  }
+  __syncthreads();
+  const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (p >= npairs) return;
   uint32_t i, j;
   if (all_pairs) {
     tri_pair(p, ndof, i, j);
@@ -925,19 +931,20 @@ __global__ void finalize2d_kernel(const uint32_t *__restrict__ pairs, int all_pa
     i = pairs[2 * p];
     j = pairs[2 * p + 1];
   }
-  const double nd = (t + 1.0) * (double)P.step_size;
-  const double X = (double)sclnc[idx] * P.fix_inv;
-  const double L = lsum[((uint64_t)i * P.nschemes + scheme) * P.nsteps + t] +
-                   lsum[((uint64_t)j * P.nschemes + scheme) * P.nsteps + t];
   // log(n A) = log n + log w_i + log w_j (per-step and per-DOF logs hoisted)
-  const double S = logw[(uint64_t)ndof * P.nschemes + t] +
-                   logw[(uint64_t)i * P.nschemes + scheme] + logw[(uint64_t)j * P.nschemes + scheme] +
-                   (L - X) / nd;
+  const double lw = logw[(uint64_t)i * P.nschemes + scheme] + logw[(uint64_t)j * P.nschemes + scheme];
+  const double *li = lsum + ((uint64_t)i * P.nschemes + scheme) * P.nsteps;
+  const double *lj = lsum + ((uint64_t)j * P.nschemes + scheme) * P.nsteps;
   const uint64_t per = (uint64_t)P.nests * P.nschemes * P.nsteps;
-  for (int e = 0; e < P.nests; ++e) {
-    double v = S;
-    if (P.ests[e] == 1) v += ((double)nnz[idx] - 1.0) / (2.0 * nd);
-    s2[p * per + ((uint64_t)e * P.nschemes + scheme) * P.nsteps + t] = v;
+  for (int t = 0; t < P.nsteps; ++t) {
+    const uint64_t idx = p * P.nsteps + t;
+    const double X = (double)sclnc[idx] * P.fix_inv;
+    const double S = log_n[t] + lw + (li[t] + lj[t] - X) * inv_n[t];
+    for (int e = 0; e < P.nests; ++e) {
+      double v = S;
+      if (P.ests[e] == 1) v += ((double)nnz[idx] - 1.0) * (0.5 * inv_n[t]);
+      s2[p * per + ((uint64_t)e * P.nschemes + scheme) * P.nsteps + t] = v;
+    }
   }
 }
 
@@ -1289,7 +1296,7 @@ int launch_finalize2d(centre_ctx *ctx, const EntParams &P, int scheme, const uin
   if (!d_logw) return st;
   // the table is rebuilt for each scheme (the same buffer serves all)
   logw_kernel<<<(unsigned)((nl + 255) / 256), 256, 0, ctx->stream>>>(d_ext, ndof, P, d_logw);
-  finalize2d_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(
+  finalize2d_kernel<<<(unsigned)((npairs + 255) / 256), 256, 0, ctx->stream>>>(
       d_pairs, all_pairs, ndof, d_logw, d_lsum, d_sclnc, d_nnz, P, scheme, npairs, d_s2);
   ctx->launches += 2;
   CENTRE_CUDA(ctx, cudaGetLastError());
@@ -1306,7 +1313,7 @@ int launch_finalize2d_into(centre_ctx *ctx, const EntParams &P, int scheme, uint
   if (total == 0) return CENTRE_OK;
   const uint64_t nl = (uint64_t)ndof * P.nschemes + P.nsteps;
   logw_kernel<<<(unsigned)((nl + 255) / 256), 256, 0, ctx->stream>>>(d_ext, ndof, P, d_logw);
-  finalize2d_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(
+  finalize2d_kernel<<<(unsigned)((npairs + 255) / 256), 256, 0, ctx->stream>>>(
       nullptr, 1, ndof, d_logw, d_lsum, d_sclnc, d_nnz, P, scheme, npairs, d_s2);
   ctx->launches += 2;
   CENTRE_CUDA(ctx, cudaGetLastError());
