@@ -362,6 +362,11 @@ def run_ours(args):
         "gpu_launches": launches,
     }
     s2_by_form = {("tc" if uses_tc else "histogram"): s2}
+    # end to end right after the device-resident steps, before the other
+    # count form's comparison run (seconds of tensor-core work); it leaves
+    # the device outputs above untouched
+    if not args.no_e2e:
+        out["e2e"] = run_e2e(ctx, tr, args, w, world, dist, dev)
     if args.compare_atomic:
         # both count forms on the same data (the metric compares them): the
         # one the timed steps did not use runs one more (warm, timed) step
@@ -393,8 +398,6 @@ def run_ours(args):
     if clocks:
         out["clocks"] = clocks
 
-    if not args.no_e2e:
-        out["e2e"] = run_e2e(ctx, tr, args, w, world, dist, dev)
     if world == 1 and not args.no_screen:
         # the learned screen on the 5000-atom chain (two timed steps after
         # one warm-up), carried as a sub-record of the default line
@@ -444,31 +447,51 @@ def run_e2e(ctx, tr, args, w, world, dist, dev):
     form = {"auto": 0, "atomic": 1, "tc": 2}[args.form]
     p = make_params(n, NSTEPS, [NBINS], [0], True, counts_form=form)
 
+    stage_s = {"discretize": 0.0, "entropy1d": 0.0, "entropy2d": 0.0, "score": 0.0}
+
     def step():
+        # each stage call returns with its outputs in host memory
+        t = time.perf_counter()
         off = 0
         for typ, data in blocks:
             k = data.shape[0]
             ctx.discretize(typ, data, [NBINS], bins_out=bins[off:off + k], ext_out=ext[off:off + k])
             off += k
+        t1 = time.perf_counter()
         ctx.entropy1d(p, types, bins, ext, out=s1)
+        t2 = time.perf_counter()
         ctx.entropy2d(p, types, bins, ext, out=s2)
-        return ctx.score(p, types, s1, s2, None, True, True, mi_out=mi)
+        t3 = time.perf_counter()
+        res = ctx.score(p, types, s1, s2, None, True, True, mi_out=mi)
+        t4 = time.perf_counter()
+        for key, a, b in (("discretize", t, t1), ("entropy1d", t1, t2), ("entropy2d", t2, t3),
+                          ("score", t3, t4)):
+            stage_s[key] += b - a
+        return res
 
     for _ in range(2):      # warm-up (first-touch of the pinned buffers)
         step()
+    for key in stage_s:
+        stage_s[key] = 0.0
     steps = max(1, min(args.steps, 3))
     if dist:
         dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        step()
-    dt = (time.perf_counter() - t0) / steps
+    with ClockSampler(dev.index if dev.index is not None else 0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            step()
+        dt = (time.perf_counter() - t0) / steps
     dt = slowest_rank(dt, dist, dev)
     h2d = sum(b.nbytes for _, b in blocks) + 2 * bins.nbytes + 2 * ext.nbytes + s1.nbytes \
         + s2.nbytes + 3 * types.nbytes
     d2h = bins.nbytes + ext.nbytes + s1.nbytes + s2.nbytes + mi.nbytes
-    return {"value": world * npairs / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3, "steps": steps}
+    out = {"value": world * npairs / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3, "steps": steps,
+           "stage_wall_ms": {k: v / steps * 1e3 for k, v in stage_s.items()}}
+    clocks = clk.summary()
+    if clocks:
+        out["clocks"] = clocks
+    return out
 
 
 # ----------------------------------------------- batched trajectories ----
