@@ -25,8 +25,12 @@ stores inputs and outputs:
   hist_tor1d_ref.json/.npz  header and first records of the reference's
                       histogram dump test_examples/example-2/outfiles-h-ref/
                       hist_tor-1d.nc
+  example1_binfiles.json  SHA-256 and size of example-1's bin_*.nc files, so
+                      the bin-file writer is checked byte for byte without
+                      the reference checkout
 
     python tests/golden/make_golden.py example1     # only the example-1 fixtures
+    python tests/golden/make_golden.py binhash      # only the bin-file hashes
     python tests/golden/make_golden.py hist         # only the histogram-dump fixture
 """
 from __future__ import annotations
@@ -191,6 +195,19 @@ def make_example1():
     np.savez_compressed(os.path.join(HERE, "example1_entcontri.npz"), **ent)
 
 
+def make_bin_hashes():
+    import hashlib
+    base = os.path.join(REF, "test_examples", "example-1", "outfiles-h-ref")
+    out = {}
+    for t in ("bonds", "angles", "torsions"):
+        with open(os.path.join(base, f"bin_{t}.nc"), "rb") as f:
+            raw = f.read()
+        out[t] = {"sha256": hashlib.sha256(raw).hexdigest(), "bytes": len(raw)}
+    out["source"] = "test_examples/example-1/outfiles-h-ref/bin_*.nc (shaileshp51/centre)"
+    with open(os.path.join(HERE, "example1_binfiles.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
 def make_hist():
     """Header and first records of the reference's histogram dump
     test_examples/example-2/outfiles-h-ref/hist_tor-1d.nc (CDF-5, written by
@@ -225,6 +242,9 @@ if __name__ == "__main__":
     if sys.argv[1:] == ["hist"]:
         make_hist()
         sys.exit(0)
+    if sys.argv[1:] == ["binhash"]:
+        make_bin_hashes()
+        sys.exit(0)
     oracle.build(with_ref=True)
     R = oracle.Reference()
     disc = make_discretize(R)
@@ -232,5 +252,6 @@ if __name__ == "__main__":
     make_mst(R)
     make_vmkde(R)
     make_example1()
+    make_bin_hashes()
     make_hist()
     print("fixtures written to", HERE)

@@ -24,6 +24,24 @@ def test_roundtrip_bins(tmp_path):
     assert sch.tolist() == [30]
 
 
+def test_bin_files_hash_like_the_reference(tmp_path):
+    """The writer, fed example-1's bins, extremes and DOF ids, produces files
+    whose SHA-256 and size are those of the reference's own bin_*.nc."""
+    import hashlib
+    import json
+    d = np.load(os.path.join(GOLDEN, "example1.npz"))
+    with open(os.path.join(GOLDEN, "example1.json")) as f:
+        schemes = json.load(f)["schemes"]
+    with open(os.path.join(GOLDEN, "example1_binfiles.json")) as f:
+        want = json.load(f)
+    for t, c in (("bonds", "B"), ("angles", "A"), ("torsions", "T")):
+        out = tmp_path / f"bin_{t}.nc"
+        cdf5.write_bins(str(out), c, d[f"{t}_dimid"], d[f"{t}_ext"], d[f"{t}_coord"], schemes)
+        raw = out.read_bytes()
+        assert len(raw) == want[t]["bytes"], t
+        assert hashlib.sha256(raw).hexdigest() == want[t]["sha256"], t
+
+
 @pytest.mark.skipif(not os.environ.get("CENTRE_REFERENCE_ROOT") or not os.path.isdir(REFDIR),
                     reason="CENTRE_REFERENCE_ROOT unset or its example files absent")
 def test_reference_bin_file_is_reproduced_byte_for_byte(tmp_path):
